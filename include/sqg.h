@@ -1,0 +1,131 @@
+/*
+ * sqg.h — C ABI of the GB300 engine for SQUANDER's decomposition hot path:
+ * the cost and gradient of a parametric gate circuit applied to a 2^n x cols
+ * complex128 target (SQUANDER hands the decomposer U^dagger and minimises
+ * f = 1 - Re Tr(C(theta) U^dagger)/cols by default).
+ *
+ * Conventions (identical to SQUANDER):
+ *   - matrices are row-major interleaved complex128 {re, im}; row stride and batch
+ *     stride are counted in complex elements; rows = 2^qbit_num;
+ *   - qubit q is bit q of the row index (LSB = qubit 0);
+ *   - gates[0] is applied first: C = G_{L-1} ... G_0;
+ *   - parameters are contiguous in gate order; U3 stores (theta/2, phi, lambda),
+ *     RX/RY/RZ/CRY store theta/2; kernels use sin/cos of the stored value.
+ *
+ * Every pointer argument named *_dev is device memory owned by the caller; the
+ * engine allocates nothing.  Calls are asynchronous on the given CUDA stream
+ * (cudaStream_t passed as void*, NULL = legacy default stream) and return a status
+ * code; no C++ exception crosses this boundary.  A circuit handle is immutable after
+ * creation and may be used from several threads and streams at once.
+ */
+#ifndef SQG_H
+#define SQG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define SQG_OK 0
+#define SQG_ERR_INVALID_ARGUMENT 1
+#define SQG_ERR_UNSUPPORTED 2
+#define SQG_ERR_WORKSPACE 3
+#define SQG_ERR_CUDA 4
+#define SQG_ERR_PARAMETER_COUNT 5
+
+/* Gate type ids, equal to SQUANDER's gate_type enum (src-cpp/gates/include/Gate.h:37-50). */
+#define SQG_CZ 4
+#define SQG_CNOT 5
+#define SQG_U3 7
+#define SQG_RY 8
+#define SQG_RX 9
+#define SQG_RZ 10
+#define SQG_CRY 14
+
+/* Cost-function variants, equal to SQUANDER's cost_function_type
+ * (src-cpp/decomposition/include/Optimization_Interface.h:43-45). */
+#define SQG_FROBENIUS_NORM 0
+#define SQG_HILBERT_SCHMIDT_TEST 3
+#define SQG_INFIDELITY 9
+
+/* One gate.  control = -1 for uncontrolled gates.  param_start is the index of the
+ * gate's first parameter in the parameter vector (Gates_block::add_gate,
+ * src-cpp/gates/Gates_block.cpp:2500-2525). */
+typedef struct sqg_gate {
+  int32_t type;
+  int32_t target;
+  int32_t control;
+  int32_t param_start;
+} sqg_gate;
+
+typedef struct sqg_circuit sqg_circuit;
+
+/* Human-readable text of a status code, or of the last error on this thread. */
+const char* sqg_status_string(int status);
+const char* sqg_last_error(void);
+
+/* Builds a circuit handle from a flat gate list (nested SQUANDER blocks are flattened
+ * by the caller in order).  Replaces the gate structure a decomposition receives via
+ * set_Gate_Structure (squander/decomposition/qgd_N_Qubit_Decompositions_Wrapper.cpp:899)
+ * and the gate list of Gates_block (src-cpp/gates/Gates_block.cpp:2500).  qbit_num
+ * 1..13.  Copies the gate table to the current device. */
+int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_circuit** out);
+int sqg_circuit_destroy(sqg_circuit* circuit);
+int sqg_circuit_param_num(const sqg_circuit* circuit);
+int sqg_circuit_qbit_num(const sqg_circuit* circuit);
+int sqg_circuit_gate_num(const sqg_circuit* circuit);
+
+/* Workspace bytes needed by sqg_cost_grad for this circuit, batch and target width. */
+size_t sqg_cost_grad_workspace_bytes(const sqg_circuit* circuit, int batch, int cols, int with_grad);
+
+/* Cost and (optionally) gradient of `batch` parameter vectors.
+ *   theta_dev   batch x P doubles (row stride P);
+ *   target_dev  rows x cols complex128 (U^dagger), shared by all instances when
+ *               target_batch_stride == 0, else one per instance at that stride;
+ *   cost_dev    batch doubles;  grad_dev  batch x P doubles or NULL (cost only).
+ * Replaces Optimization_Interface::optimization_problem (Optimization_Interface.cpp:634-668),
+ * optimization_problem_batched (:940-1033) and optimization_problem_combined_non_static
+ * (:1145-1485) of the CPU reference, for the cost variants listed above.  The gradient
+ * is the adjoint (reverse-sweep) gradient; checkpoint_interval > 0 stores the forward
+ * state every that many gates in the workspace and restores it during the reverse sweep
+ * instead of relying on uncomputation alone (0 = pure uncomputation). */
+int sqg_cost_grad(const sqg_circuit* circuit, const double* theta_dev, int batch, const void* target_dev, int cols,
+                  long long target_batch_stride, int trace_offset, int cost_variant, double* cost_dev,
+                  double* grad_dev, int checkpoint_interval, void* workspace_dev, size_t workspace_bytes,
+                  void* stream);
+size_t sqg_cost_grad_checkpoint_workspace_bytes(const sqg_circuit* circuit, int batch, int cols,
+                                                int checkpoint_interval);
+
+/* Workspace bytes needed by sqg_apply. */
+size_t sqg_apply_workspace_bytes(const sqg_circuit* circuit, int batch);
+
+/* In-place left application M_b <- C(theta_b) M_b for `batch` matrices of rows x cols
+ * (row stride `stride`, batch stride `batch_stride`, both in complex elements).
+ * fused = 1: every gate applied to shared-memory column tiles in one pass over the
+ * matrix; fused = 0: one pass over the matrix per gate.  Replaces Gates_block::apply_to
+ * (src-cpp/gates/Gates_block.cpp:606-710) and Circuit.apply_to
+ * (squander/gates/qgd_Circuit.py:546). */
+int sqg_apply(const sqg_circuit* circuit, const double* theta_dev, int batch, void* mtx_dev, int cols,
+              long long stride, long long batch_stride, int fused, void* workspace_dev, size_t workspace_bytes,
+              void* stream);
+
+/* In-place right application M <- M C(theta) (cols = 2^qbit_num).  Replaces
+ * Gates_block::apply_from_right (src-cpp/gates/Gates_block.cpp:885-935). */
+int sqg_apply_from_right(const sqg_circuit* circuit, const double* theta_dev, void* mtx_dev, int rows,
+                         long long stride, void* workspace_dev, size_t workspace_bytes, void* stream);
+
+/* Forward matrix and all P derivative matrices: out_dev holds P+1 matrices of
+ * rows x cols (dense, stride cols): out[0] = C(theta) target, out[1+k] = dC/dtheta_k target.
+ * Replaces Optimization_Interface::optimization_problem_combined_unitary
+ * (Optimization_Interface.cpp:1525-1547) and Gates_block::apply_to_combined / apply_derivate_to
+ * (src-cpp/gates/Gates_block.cpp:1012-1150, 1328-1364). */
+int sqg_combined_unitary(const sqg_circuit* circuit, const double* theta_dev, const void* target_dev, int cols,
+                         void* out_dev, void* workspace_dev, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SQG_H */

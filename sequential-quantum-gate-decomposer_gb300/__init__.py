@@ -1,0 +1,25 @@
+"""GB300-native engine for SQUANDER's decomposition hot path.
+
+The cost ``1 - Re Tr(C(theta) U^dagger)/cols`` (and the HILBERT_SCHMIDT_TEST /
+INFIDELITY variants) of a parametric U3/RX/RY/RZ/CNOT/CZ/CRY circuit and its adjoint
+gradient run in hand-written sm_103a CUDA kernels (libsqg.so, C ABI in include/sqg.h).
+This package mirrors the reference's Python surface for that path:
+``Circuit`` (squander.Circuit) and ``N_Qubit_Decomposition_custom``.
+
+The directory name contains hyphens, so import it with
+``importlib.import_module("sequential-quantum-gate-decomposer_gb300")``; the package
+also registers itself under the alias ``sqg_gb300``.
+"""
+import sys as _sys
+
+from ._native import SQGError, build
+from .circuit import CNOT, CRY, CZ, RX, RY, RZ, U3, Circuit
+from .decomposition import N_Qubit_Decomposition_custom
+from .evaluator import (FROBENIUS_NORM, HILBERT_SCHMIDT_TEST, INFIDELITY, CircuitCost, CostEvaluator,
+                        circuit_cost)
+
+_sys.modules.setdefault("sqg_gb300", _sys.modules[__name__])
+
+__all__ = ["Circuit", "N_Qubit_Decomposition_custom", "CostEvaluator", "CircuitCost", "circuit_cost", "SQGError",
+           "build", "FROBENIUS_NORM", "HILBERT_SCHMIDT_TEST", "INFIDELITY", "U3", "RX", "RY", "RZ", "CNOT", "CZ",
+           "CRY"]

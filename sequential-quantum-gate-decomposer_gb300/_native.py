@@ -1,0 +1,136 @@
+"""Loader and ctypes bindings of the engine's C ABI (include/sqg.h).
+
+The shared library ``libsqg.so`` is built in-tree by :func:`build` with nvcc for
+sm_103a.  There is no CPU fallback: every entry point of this package raises if the
+library or a CUDA device is missing.
+"""
+import ctypes
+import os
+import subprocess
+import sys
+import threading
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+INCLUDE = os.path.join(REPO_DIR, "include")
+LIB_PATH = os.path.join(PKG_DIR, "libsqg.so")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+
+CU_SOURCES = ["engine.cu"]
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
+
+# status codes (sqg.h)
+SQG_OK = 0
+STATUS_TEXT = {0: "ok", 1: "invalid argument", 2: "unsupported configuration", 3: "workspace too small",
+               4: "CUDA error", 5: "wrong number of parameters"}
+
+
+class SQGError(RuntimeError):
+    """Error reported by the engine through a non-zero status code."""
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def _sources():
+    return [os.path.join(CSRC, s) for s in CU_SOURCES]
+
+
+def _deps():
+    deps = _sources() + [os.path.join(INCLUDE, "sqg.h")]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    return deps
+
+
+def needs_build():
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    return any(os.path.getmtime(d) > t for d in _deps())
+
+
+def build(force=False, verbose=False):
+    """Compile every CUDA translation unit for sm_103a (in parallel) and link libsqg.so."""
+    if not force and not needs_build():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    procs = []
+    objs = []
+    for src in _sources():
+        obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+        objs.append(obj)
+        cmd = [nvcc] + NVCC_FLAGS + ["-I", INCLUDE, "-c", "-o", obj, src]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("nvcc failed: %s\n%s" % (" ".join(cmd), out.decode(errors="replace")))
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs + [
+        "-lcudart"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def _declare(lib):
+    c_int, c_ll, c_sz, vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_size_t, ctypes.c_void_p
+    lib.sqg_status_string.restype = ctypes.c_char_p
+    lib.sqg_status_string.argtypes = [c_int]
+    lib.sqg_last_error.restype = ctypes.c_char_p
+    lib.sqg_last_error.argtypes = []
+    lib.sqg_circuit_create.argtypes = [c_int, vp, c_int, ctypes.POINTER(vp)]
+    lib.sqg_circuit_destroy.argtypes = [vp]
+    for f in ("sqg_circuit_param_num", "sqg_circuit_qbit_num", "sqg_circuit_gate_num"):
+        getattr(lib, f).argtypes = [vp]
+    lib.sqg_cost_grad_workspace_bytes.restype = c_sz
+    lib.sqg_cost_grad_workspace_bytes.argtypes = [vp, c_int, c_int, c_int]
+    lib.sqg_cost_grad_checkpoint_workspace_bytes.restype = c_sz
+    lib.sqg_cost_grad_checkpoint_workspace_bytes.argtypes = [vp, c_int, c_int, c_int]
+    lib.sqg_cost_grad.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_int, c_int, vp, vp, c_int, vp, c_sz, vp]
+    lib.sqg_apply_workspace_bytes.restype = c_sz
+    lib.sqg_apply_workspace_bytes.argtypes = [vp, c_int]
+    lib.sqg_apply.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_ll, c_int, vp, c_sz, vp]
+    lib.sqg_apply_from_right.argtypes = [vp, vp, vp, c_int, c_ll, vp, c_sz, vp]
+    lib.sqg_combined_unitary.argtypes = [vp, vp, vp, c_int, vp, vp, c_sz, vp]
+
+
+def lib():
+    """The loaded engine library (built on first use if absent)."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if needs_build():
+                    build()
+                l = ctypes.CDLL(LIB_PATH)
+                _declare(l)
+                _lib = l
+    return _lib
+
+
+def check(status, what=""):
+    if status != SQG_OK:
+        msg = lib().sqg_last_error().decode(errors="replace")
+        raise SQGError("%s: %s (%s)" % (what, STATUS_TEXT.get(status, "status %d" % status), msg))
+
+
+EXPORTED_SYMBOLS = [
+    "sqg_status_string", "sqg_last_error", "sqg_circuit_create", "sqg_circuit_destroy", "sqg_circuit_param_num",
+    "sqg_circuit_qbit_num", "sqg_circuit_gate_num", "sqg_cost_grad_workspace_bytes",
+    "sqg_cost_grad_checkpoint_workspace_bytes", "sqg_cost_grad", "sqg_apply_workspace_bytes", "sqg_apply",
+    "sqg_apply_from_right", "sqg_combined_unitary",
+]

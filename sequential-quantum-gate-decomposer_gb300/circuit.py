@@ -1,0 +1,246 @@
+"""Gate structures: a drop-in for ``squander.Circuit`` (squander/gates/qgd_Circuit.py)
+restricted to the hot-path gate set U3, RX, RY, RZ, CNOT, CZ, CRY and nested circuits.
+
+Conventions follow SQUANDER: gates are appended in order and gates[0] acts first
+(Gates_block::add_gate, src-cpp/gates/Gates_block.cpp:2500-2525); two-qubit gates take
+``(target, control)``; parameters are contiguous in gate order, U3 stores
+(theta/2, phi, lambda), the rotations store theta/2.  Every numerical method runs on the
+GPU through libsqg.so.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _device as dev
+from . import _native
+
+CZ, CNOT, U3, RY, RX, RZ, CRY = 4, 5, 7, 8, 9, 10, 14
+GATE_NAMES = {CZ: "CZ", CNOT: "CNOT", U3: "U3", RY: "RY", RX: "RX", RZ: "RZ", CRY: "CRY"}
+PARAM_NUM = {CZ: 0, CNOT: 0, U3: 3, RY: 1, RX: 1, RZ: 1, CRY: 1}
+
+
+class NativeCircuit:
+    """Owning wrapper of an ``sqg_circuit*`` handle."""
+
+    def __init__(self, qbit_num, records):
+        lib = _native.lib()
+        recs = np.ascontiguousarray(np.asarray(records, dtype=np.int32).reshape(-1, 4))
+        h = ctypes.c_void_p()
+        _native.check(lib.sqg_circuit_create(int(qbit_num), recs.ctypes.data if recs.size else None, recs.shape[0],
+                                             ctypes.byref(h)), "sqg_circuit_create")
+        self.handle = h.value
+        self.qbit_num = int(qbit_num)
+        self.param_num = lib.sqg_circuit_param_num(self.handle)
+        self.gate_num = recs.shape[0]
+        self.records = recs
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            try:
+                _native.lib().sqg_circuit_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+class Circuit:
+    """Ordered parametric gate list on ``qbit_num`` qubits (SQUANDER ``qgd_Circuit``)."""
+
+    def __init__(self, qbit_num):
+        if int(qbit_num) < 1:
+            raise ValueError("qbit_num must be positive")
+        self.qbit_num = int(qbit_num)
+        self._gates = []  # (type, target, control)
+        self._native = None
+        self._ws = dev.Workspace()
+        self.min_fusion = -1
+
+    # ---- structure -------------------------------------------------------------------
+    def _check_qubit(self, q, what):
+        if not (0 <= int(q) < self.qbit_num):
+            raise ValueError("%s qubit index %d out of range for %d qubits" % (what, q, self.qbit_num))
+
+    def _add(self, gtype, target, control=-1):
+        self._check_qubit(target, "target")
+        if control != -1:
+            self._check_qubit(control, "control")
+            if control == target:
+                raise ValueError("control and target qubits must differ")
+        self._gates.append((gtype, int(target), int(control)))
+        self._native = None
+
+    def add_U3(self, target_qbit):
+        self._add(U3, target_qbit)
+
+    def add_RX(self, target_qbit):
+        self._add(RX, target_qbit)
+
+    def add_RY(self, target_qbit):
+        self._add(RY, target_qbit)
+
+    def add_RZ(self, target_qbit):
+        self._add(RZ, target_qbit)
+
+    def add_CNOT(self, target_qbit, control_qbit):
+        self._add(CNOT, target_qbit, control_qbit)
+
+    def add_CZ(self, target_qbit, control_qbit):
+        self._add(CZ, target_qbit, control_qbit)
+
+    def add_CRY(self, target_qbit, control_qbit):
+        self._add(CRY, target_qbit, control_qbit)
+
+    def add_Circuit(self, other):
+        """Append a sub-circuit; its gates are flattened in order (SQUANDER keeps a
+        nested block whose parameters are likewise contiguous)."""
+        if other.qbit_num > self.qbit_num:
+            raise ValueError("sub-circuit spans more qubits than the circuit")
+        self._gates.extend(other._gates)
+        self._native = None
+
+    def get_Qbit_Num(self):
+        return self.qbit_num
+
+    def get_Parameter_Num(self):
+        return sum(PARAM_NUM[g[0]] for g in self._gates)
+
+    def get_Gate_Num(self):
+        return len(self._gates)
+
+    def get_Gates(self):
+        out, p = [], 0
+        for t, tg, c in self._gates:
+            d = {"type": GATE_NAMES[t], "target_qbit": tg, "parameter_start_index": p}
+            if c >= 0:
+                d["control_qbit"] = c
+            out.append(d)
+            p += PARAM_NUM[t]
+        return out
+
+    def get_Gate_Nums(self):
+        nums = {}
+        for t, _, _ in self._gates:
+            nums[GATE_NAMES[t]] = nums.get(GATE_NAMES[t], 0) + 1
+        return nums
+
+    def get_Parameter_Start_Index(self):
+        return 0
+
+    def set_min_fusion(self, min_fusion):
+        """Recorded for API compatibility: the engine always applies the whole circuit to
+        shared-memory column tiles, which subsumes SQUANDER's k-qubit fusion."""
+        self.min_fusion = int(min_fusion)
+
+    def gate_records(self):
+        """(L, 4) int32 array of (type, target, control, param_start)."""
+        recs, p = [], 0
+        for t, tg, c in self._gates:
+            recs.append((t, tg, c, p))
+            p += PARAM_NUM[t]
+        return np.asarray(recs, dtype=np.int32).reshape(-1, 4)
+
+    def native(self):
+        if self._native is None:
+            self._native = NativeCircuit(self.qbit_num, self.gate_records())
+        return self._native
+
+    # ---- device-level operations (torch CUDA tensors in, results in place) -----------
+    def _params_dev(self, parameters):
+        p = dev.to_device_real(parameters).reshape(-1)
+        if p.numel() != self.get_Parameter_Num():
+            raise ValueError("expected %d parameters, got %d" % (self.get_Parameter_Num(), p.numel()))
+        return p
+
+    def apply_to_device(self, params_dev, mtx_dev, fused=True, stream=None):
+        """In place M <- C(params) M for a CUDA complex128 tensor (rows x cols, or a batch
+        (B, rows, cols) with params (B, P))."""
+        nc = self.native()
+        B = mtx_dev.shape[0] if mtx_dev.dim() == 3 else 1
+        rows, cols = mtx_dev.shape[-2], mtx_dev.shape[-1]
+        if rows != (1 << self.qbit_num):
+            raise ValueError("Gates_block::apply_to: Wrong input size in Gates_block gate apply.")
+        if not mtx_dev.is_contiguous():
+            raise ValueError("matrix must be contiguous")
+        ws_bytes = _native.lib().sqg_apply_workspace_bytes(nc.handle, B)
+        ws = self._ws.get(ws_bytes)
+        _native.check(_native.lib().sqg_apply(nc.handle, dev.ptr(params_dev) if params_dev.numel() else None, B,
+                                              dev.ptr(mtx_dev), cols, cols, rows * cols, 1 if fused else 0,
+                                              dev.ptr(ws), ws.numel(), dev.stream_ptr(stream)), "sqg_apply")
+        return mtx_dev
+
+    # ---- SQUANDER-compatible host API (numpy in, numpy out / in place) ---------------
+    def get_Matrix(self, parameters_mtx, is_f32=False):
+        if is_f32:
+            raise NotImplementedError("the GB300 engine computes in FP64 only")
+        self.native()
+        params = self._params_dev(parameters_mtx)
+        m = dev.torch.eye(1 << self.qbit_num, dtype=dev.torch.complex128, device="cuda")
+        self.apply_to_device(params, m)
+        return m.cpu().numpy()
+
+    def _check_mtx(self, unitary_mtx):
+        if not isinstance(unitary_mtx, np.ndarray) or unitary_mtx.dtype != np.complex128:
+            raise TypeError("input matrix must be a complex128 numpy array")
+        if unitary_mtx.ndim == 1:
+            unitary_mtx = unitary_mtx.reshape(-1, 1)
+        if unitary_mtx.shape[0] != (1 << self.qbit_num):
+            raise ValueError("Gates_block::apply_to: Wrong input size in Gates_block gate apply.")
+        return unitary_mtx
+
+    def apply_to(self, parameters_mtx, unitary_mtx, parallel=1, is_f32=False):
+        """In place ``unitary_mtx <- C(parameters) unitary_mtx`` (qgd_Circuit.py:546)."""
+        if is_f32:
+            raise NotImplementedError("the GB300 engine computes in FP64 only")
+        view = self._check_mtx(unitary_mtx)
+        if np.asarray(parameters_mtx).dtype != np.float64:
+            raise TypeError("parameters must be float64")
+        params = self._params_dev(parameters_mtx)
+        m = dev.to_device_complex(np.ascontiguousarray(view))
+        self.apply_to_device(params, m)
+        view[...] = m.cpu().numpy()
+
+    def apply_from_right(self, parameters_mtx, unitary_mtx, parallel=1, is_f32=False):
+        """In place ``unitary_mtx <- unitary_mtx C(parameters)`` (qgd_Circuit.py:559)."""
+        if is_f32:
+            raise NotImplementedError("the GB300 engine computes in FP64 only")
+        if not isinstance(unitary_mtx, np.ndarray) or unitary_mtx.dtype != np.complex128:
+            raise TypeError("input matrix must be a complex128 numpy array")
+        if unitary_mtx.shape[-1] != (1 << self.qbit_num):
+            raise ValueError("Gates_block::apply_from_right: Wrong matrix size")
+        params = self._params_dev(parameters_mtx)
+        nc = self.native()
+        m = dev.to_device_complex(np.ascontiguousarray(unitary_mtx))
+        ws = self._ws.get(_native.lib().sqg_apply_workspace_bytes(nc.handle, 1))
+        _native.check(_native.lib().sqg_apply_from_right(nc.handle, dev.ptr(params) if params.numel() else None,
+                                                         dev.ptr(m), m.shape[0], m.shape[1], dev.ptr(ws),
+                                                         ws.numel(), dev.stream_ptr()), "sqg_apply_from_right")
+        unitary_mtx[...] = m.cpu().numpy()
+
+    def apply_to_combined(self, parameters_mtx, unitary_mtx, parallel=1, is_f32=False):
+        """[C U, dC/dp_0 U, ...] (qgd_Circuit.py:597)."""
+        if is_f32:
+            raise NotImplementedError("the GB300 engine computes in FP64 only")
+        if np.asarray(parameters_mtx).dtype != np.float64:
+            raise TypeError("parameters must be float64")
+        view = self._check_mtx(unitary_mtx)
+        params = self._params_dev(parameters_mtx)
+        out = combined_unitary_device(self.native(), params, dev.to_device_complex(np.ascontiguousarray(view)),
+                                      self._ws)
+        host = out.cpu().numpy()
+        return [host[k] for k in range(host.shape[0])]
+
+    def apply_derivate_to(self, parameters_mtx, unitary_mtx, parallel=1, is_f32=False):
+        """[dC/dp_k U for every parameter] (qgd_Circuit.py:583)."""
+        return self.apply_to_combined(parameters_mtx, unitary_mtx, parallel, is_f32)[1:]
+
+
+def combined_unitary_device(nc, params_dev, target_dev, ws):
+    """(P+1, rows, cols) CUDA tensor: the forward matrix and every derivative matrix."""
+    rows, cols = target_dev.shape
+    out = dev.torch.empty((nc.param_num + 1, rows, cols), dtype=dev.torch.complex128, device="cuda")
+    buf = ws.get(_native.lib().sqg_apply_workspace_bytes(nc.handle, 1))
+    _native.check(_native.lib().sqg_combined_unitary(nc.handle, dev.ptr(params_dev) if params_dev.numel() else None,
+                                                     dev.ptr(target_dev), cols, dev.ptr(out), dev.ptr(buf),
+                                                     buf.numel(), dev.stream_ptr()), "sqg_combined_unitary")
+    return out

@@ -1,0 +1,873 @@
+// GB300 engine for the SQUANDER decomposition hot path: cost and adjoint gradient of a
+// parametric circuit applied to a 2^n x cols complex128 target, plus forward/right
+// application and the combined-unitary parity API.  Entry points are declared in
+// include/sqg.h.
+//
+// Design (GB300-first, one GPU):
+//  * Column tiles.  Gates mix rows only, so every column of U^dagger is an independent
+//    state vector.  A CTA loads a tile of TC columns into shared memory (column-major:
+//    each column contiguous), applies ALL L gates there, and reads HBM once.  The whole
+//    circuit is fused, whatever qubits it touches (n <= 13 fits a column in 128 KB).
+//  * Adjoint gradient per column: psi = C u_j is uncomputed gate by gate with G^dagger
+//    while the co-state lambda (starting at e_{j+offset}) is propagated with G^dagger;
+//    for each parametric gate the 2x2 overlap R_ab = sum conj(lambda_a) psi_b is reduced
+//    over the tile and contracted with the derivative kernels.  O(L) passes in shared
+//    memory replace the reference's (P+1) dense derivative matrices.
+//  * FP64 is the binding resource on GB300, so the update rules (gates.cuh) minimise FP64
+//    instructions and everything else (index math, exchanges, sign flips) is integer work.
+//  * Deterministic reductions: per-tile partial traces go to the caller's workspace and
+//    are summed in a fixed order by a second kernel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sqg.h"
+#include "gates.cuh"
+
+using namespace sqg;
+
+struct sqg_circuit {
+  int n = 0, N = 0, L = 0, P = 0;
+  int device = 0;
+  Gate* d_gates = nullptr;
+  std::vector<Gate> h_gates;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int cuda_status(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return SQG_OK;
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return SQG_ERR_CUDA;
+}
+
+constexpr int kMaxThreads = 256;
+constexpr int kMaxWarps = kMaxThreads / 32;
+constexpr size_t kSmemBudgetFwd = 132 * 1024;   // column tile budget, forward only
+constexpr size_t kSmemBudgetGrad = 100 * 1024;  // psi + lambda tiles
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// -------------------------------------------------------------------------------------
+// Gate-matrix preparation: one thread per (instance, gate).  Each parameter belongs to
+// exactly one gate, so sin/cos of each stored parameter is evaluated once
+// (Gates_block.cpp:269-279 evaluates them the same way, per parameter).
+// -------------------------------------------------------------------------------------
+__global__ void k_prep(const Gate* __restrict__ gates, int L, int P, const double* __restrict__ theta,
+                       long long theta_stride, int B, GateMat* __restrict__ gm, double2* __restrict__ sc) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  int b = blockIdx.y;
+  if (g >= L || b >= B) return;
+  Gate gt = gates[g];
+  const double* th = theta + (long long)b * theta_stride + gt.pstart;
+  GateMat m;
+  m.u[0] = m.u[1] = m.u[2] = m.u[3] = make_double2(0.0, 0.0);
+  double2* scb = sc + (long long)b * P + gt.pstart;
+  if (gt.type == G_U3) {
+    double st, ct, sp, cp, sl, cl;
+    sincos(th[0], &st, &ct);
+    sincos(th[1], &sp, &cp);
+    sincos(th[2], &sl, &cl);
+    scb[0] = make_double2(st, ct);
+    scb[1] = make_double2(sp, cp);
+    scb[2] = make_double2(sl, cl);
+    double spl = sp * cl + cp * sl, cpl = cp * cl - sp * sl;
+    // gate_kernel_templates.h:509-521
+    m.u[0] = make_double2(ct, 0.0);
+    m.u[1] = make_double2(-st * cl, -st * sl);
+    m.u[2] = make_double2(st * cp, st * sp);
+    m.u[3] = make_double2(ct * cpl, ct * spl);
+  } else if (gate_param_num(gt.type) == 1) {
+    double s, c;
+    sincos(th[0], &s, &c);
+    scb[0] = make_double2(s, c);
+    m.u[0] = make_double2(c, s);
+  }
+  gm[(long long)b * L + g] = m;
+}
+
+// -------------------------------------------------------------------------------------
+// Shared-memory column-tile machinery.
+// -------------------------------------------------------------------------------------
+struct TileArgs {
+  const Gate* gates;
+  int L, P, n, N;
+  const GateMat* gm;   // [B][L]
+  const double2* sc;   // [B][P]
+  // matrix source (target or in/out matrix); element (r, c) of instance b at
+  // base + b*bstride + r*rstride + c*cstride
+  double2* mtx;
+  long long bstride, rstride, cstride;
+  int cols;          // number of vectors (columns for left application, rows for right)
+  int TC;            // vectors per tile
+  int tiles;         // tiles per instance
+  int trace_offset;  // row offset of the traced element (left application)
+  int reverse_order; // right application walks the gates from last to first
+  int orient;        // ORIENT_FWD or ORIENT_TRANS
+  double2* ws_tr;    // [B][tiles] forward trace partials
+  double2* ws_gr;    // [B][tiles][P] derivative trace partials
+  double2* ckpt;     // checkpoints [B][tiles][nck][TC][N] or null
+  int ckpt_interval;
+  int nck;
+};
+
+// Applies one gate to every vector of the tile.  s holds tc vectors of length N.
+__device__ __forceinline__ void tile_apply(double2* s, int N, int logN, int tc, const Gate& gt, const PairOp& op) {
+  const bool ctrl = gate_controlled(gt.type);
+  const int lognp = ctrl ? logN - 2 : logN - 1;
+  const int npairs = 1 << lognp;
+  const int items = tc << lognp;
+  const int step = 1 << gt.target;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    int col = it >> lognp;
+    int p = it & (npairs - 1);
+    int i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
+    double2* v = s + col * N;
+    double2 x = v[i], y = v[i + step];
+    apply_op(op, x, y);
+    v[i] = x;
+    v[i + step] = y;
+  }
+}
+
+__device__ __forceinline__ void load_tile(double2* s, const TileArgs& a, int b, int v0, int tc) {
+  const double2* base = a.mtx + (long long)b * a.bstride;
+  const int total = a.N * tc;
+  if (a.cstride == 1) {
+    // left application: vector = column, element r at row r; read rows coalesced
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+      int r = e / tc, c = e - r * tc;
+      s[c * a.N + r] = base[(long long)r * a.rstride + v0 + c];
+    }
+  } else {
+    // right application: vector = row (contiguous)
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+      int c = e / a.N, r = e - c * a.N;
+      s[c * a.N + r] = base[(long long)(v0 + c) * a.rstride + r];
+    }
+  }
+}
+
+__device__ __forceinline__ void store_tile(const double2* s, const TileArgs& a, int b, int v0, int tc) {
+  double2* base = a.mtx + (long long)b * a.bstride;
+  const int total = a.N * tc;
+  if (a.cstride == 1) {
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+      int r = e / tc, c = e - r * tc;
+      base[(long long)r * a.rstride + v0 + c] = s[c * a.N + r];
+    }
+  } else {
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+      int c = e / a.N, r = e - c * a.N;
+      base[(long long)(v0 + c) * a.rstride + r] = s[c * a.N + r];
+    }
+  }
+}
+
+// Block-wide sum of a complex value; result valid in thread 0.
+__device__ __forceinline__ double2 block_sum2(double2 v, double2* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+  if (nw == 1) return v;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double2 t = make_double2(0.0, 0.0);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < nw; k++) { t.x += red[k].x; t.y += red[k].y; }
+  __syncthreads();
+  return t;
+}
+
+// Forward (or right) application of the whole circuit to one tile; optionally writes
+// the tile back and/or the traced diagonal partial.
+template <bool WRITE_BACK, bool TRACE>
+__global__ void __launch_bounds__(kMaxThreads) k_tile_forward(TileArgs a) {
+  extern __shared__ double2 smem[];
+  double2* s = smem;
+  double2* red = smem + (size_t)a.TC * a.N;
+  const int b = blockIdx.y, tile = blockIdx.x;
+  const int v0 = tile * a.TC;
+  const int tc = min(a.TC, a.cols - v0);
+  const int logN = a.n;
+  load_tile(s, a, b, v0, tc);
+  __syncthreads();
+  const GateMat* gm = a.gm + (long long)b * a.L;
+  for (int k = 0; k < a.L; k++) {
+    int g = a.reverse_order ? a.L - 1 - k : k;
+    Gate gt = a.gates[g];
+    PairOp op = make_op(gt.type, gm[g], a.orient);
+    tile_apply(s, a.N, logN, tc, gt, op);
+    __syncthreads();
+  }
+  if (TRACE) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int c = threadIdx.x; c < tc; c += blockDim.x) {
+      int row = v0 + c + a.trace_offset;
+      double2 v = s[c * a.N + row];
+      t.x += v.x;
+      t.y += v.y;
+    }
+    t = block_sum2(t, red);
+    if (threadIdx.x == 0) a.ws_tr[(long long)b * a.tiles + tile] = t;
+  }
+  if (WRITE_BACK) store_tile(s, a, b, v0, tc);
+}
+
+// Warp reduce-scatter of 8 doubles: afterwards lane l holds the warp total of value
+// (l >> 2) & 7 (9 FP64 adds per lane instead of 40 for eight full butterflies).
+__device__ __forceinline__ double warp_reduce_scatter8(double r[8]) {
+  const int lane = threadIdx.x & 31;
+  {
+    const bool hi = lane & 16;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      double send = hi ? r[k] : r[k + 4];
+      double keep = hi ? r[k + 4] : r[k];
+      r[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+  }
+  {
+    const bool hi = lane & 8;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      double send = hi ? r[k] : r[k + 2];
+      double keep = hi ? r[k + 2] : r[k];
+      r[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+  }
+  {
+    const bool hi = lane & 4;
+    double send = hi ? r[0] : r[1];
+    double keep = hi ? r[1] : r[0];
+    r[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  double v = r[0];
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v;
+}
+
+// Cost + adjoint gradient of one (instance, tile).
+__global__ void __launch_bounds__(kMaxThreads) k_tile_adjoint(TileArgs a) {
+  extern __shared__ double2 smem[];
+  const int N = a.N, logN = a.n;
+  double2* psi = smem;
+  double2* lam = smem + (size_t)a.TC * N;
+  double* redd = reinterpret_cast<double*>(lam + (size_t)a.TC * N);  // [kMaxWarps][8]
+  double* tot = redd + kMaxWarps * 8;                                 // [8]
+  double2* red2 = reinterpret_cast<double2*>(tot + 8);                // [kMaxWarps]
+  const int b = blockIdx.y, tile = blockIdx.x;
+  const int v0 = tile * a.TC;
+  const int tc = min(a.TC, a.cols - v0);
+  const int nw = (blockDim.x + 31) >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t tile_elems = (size_t)a.TC * N;
+  double2* ck = a.ckpt ? a.ckpt + ((long long)b * a.tiles + tile) * a.nck * tile_elems : nullptr;
+
+  load_tile(psi, a, b, v0, tc);
+  // lambda_j = e_{j + offset}
+  for (int e = threadIdx.x; e < tc * N; e += blockDim.x) {
+    int c = e / N, r = e - c * N;
+    lam[e] = make_double2(r == v0 + c + a.trace_offset ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  const GateMat* gm = a.gm + (long long)b * a.L;
+  const double2* scb = a.sc + (long long)b * a.P;
+  // forward sweep
+  for (int g = 0; g < a.L; g++) {
+    Gate gt = a.gates[g];
+    PairOp op = make_op(gt.type, gm[g], ORIENT_FWD);
+    tile_apply(psi, N, logN, tc, gt, op);
+    __syncthreads();
+    if (ck && (g + 1) % a.ckpt_interval == 0 && (g + 1) / a.ckpt_interval <= a.nck) {
+      double2* dst = ck + (size_t)((g + 1) / a.ckpt_interval - 1) * tile_elems;
+      for (int e = threadIdx.x; e < tc * N; e += blockDim.x) dst[e] = psi[e];
+    }
+  }
+  // forward trace partial
+  {
+    double2 t = make_double2(0.0, 0.0);
+    for (int c = threadIdx.x; c < tc; c += blockDim.x) {
+      double2 v = psi[c * N + v0 + c + a.trace_offset];
+      t.x += v.x;
+      t.y += v.y;
+    }
+    t = block_sum2(t, red2);
+    if (threadIdx.x == 0) a.ws_tr[(long long)b * a.tiles + tile] = t;
+  }
+  double2* wgr = a.ws_gr + ((long long)b * a.tiles + tile) * a.P;
+  // reverse sweep
+  for (int g = a.L - 1; g >= 0; g--) {
+    Gate gt = a.gates[g];
+    if (ck && (g + 1) % a.ckpt_interval == 0 && (g + 1) / a.ckpt_interval <= a.nck && g + 1 < a.L) {
+      // psi currently holds the uncomputed state after gate g; restore the stored one
+      const double2* src = ck + (size_t)((g + 1) / a.ckpt_interval - 1) * tile_elems;
+      __syncthreads();
+      for (int e = threadIdx.x; e < tc * N; e += blockDim.x) psi[e] = src[e];
+      __syncthreads();
+    }
+    PairOp op = make_op(gt.type, gm[g], ORIENT_ADJ);
+    const int np = gate_param_num(gt.type);
+    if (np == 0) {
+      tile_apply(psi, N, logN, tc, gt, op);
+      tile_apply(lam, N, logN, tc, gt, op);
+      __syncthreads();
+      continue;
+    }
+    const bool ctrl = gate_controlled(gt.type);
+    const int lognp = ctrl ? logN - 2 : logN - 1;
+    const int npairs = 1 << lognp;
+    const int items = tc << lognp;
+    const int step = 1 << gt.target;
+    double r[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) r[k] = 0.0;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      int col = it >> lognp;
+      int p = it & (npairs - 1);
+      int i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
+      double2* ps = psi + col * N;
+      double2* ls = lam + col * N;
+      double2 x = ps[i], y = ps[i + step];
+      apply_op(op, x, y);  // psi before gate g
+      ps[i] = x;
+      ps[i + step] = y;
+      double2 lx = ls[i], ly = ls[i + step];
+      // R_ab += conj(lambda_a) psi_b
+      r[0] = fma(lx.x, x.x, fma(lx.y, x.y, r[0]));
+      r[1] = fma(lx.x, x.y, fma(-lx.y, x.x, r[1]));
+      r[2] = fma(lx.x, y.x, fma(lx.y, y.y, r[2]));
+      r[3] = fma(lx.x, y.y, fma(-lx.y, y.x, r[3]));
+      r[4] = fma(ly.x, x.x, fma(ly.y, x.y, r[4]));
+      r[5] = fma(ly.x, x.y, fma(-ly.y, x.x, r[5]));
+      r[6] = fma(ly.x, y.x, fma(ly.y, y.y, r[6]));
+      r[7] = fma(ly.x, y.y, fma(-ly.y, y.x, r[7]));
+      apply_op(op, lx, ly);  // lambda before gate g
+      ls[i] = lx;
+      ls[i + step] = ly;
+    }
+    double v = warp_reduce_scatter8(r);
+    if (nw == 1) {
+      if ((lane & 3) == 0) tot[lane >> 2] = v;
+    } else if ((lane & 3) == 0) {
+      redd[warp * 8 + (lane >> 2)] = v;
+    }
+    __syncthreads();
+    if (nw > 1 && threadIdx.x < 8) {
+      double t = 0.0;
+      for (int w = 0; w < nw; w++) t += redd[w * 8 + threadIdx.x];
+      tot[threadIdx.x] = t;
+    }
+    if (nw > 1) __syncthreads();
+    if (threadIdx.x < np) {
+      double2 D[4];
+      deriv_kernel(gt.type, scb + gt.pstart, threadIdx.x, D);
+      // T = sum_ab D_ab R_ab
+      double tr = 0.0, ti = 0.0;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        double rr = tot[2 * k], ri = tot[2 * k + 1];
+        tr = fma(D[k].x, rr, fma(-D[k].y, ri, tr));
+        ti = fma(D[k].x, ri, fma(D[k].y, rr, ti));
+      }
+      wgr[gt.pstart + threadIdx.x] = make_double2(tr, ti);
+    }
+  }
+}
+
+// Sums the per-tile partials in a fixed order and applies the cost-variant epilogue of
+// the reference (Optimization_Interface.cpp:677-735 for the cost, :1397-1458 for the
+// gradient components).
+__global__ void k_finish(const double2* __restrict__ ws_tr, const double2* __restrict__ ws_gr, int tiles, int P,
+                         int cols, int variant, double* __restrict__ cost, double* __restrict__ grad) {
+  const int b = blockIdx.x;
+  double2 tr = make_double2(0.0, 0.0);
+  for (int t = 0; t < tiles; t++) {
+    double2 v = ws_tr[(long long)b * tiles + t];
+    tr.x += v.x;
+    tr.y += v.y;
+  }
+  if (blockIdx.y == 0 && threadIdx.x == 0) {
+    double f;
+    if (variant == SQG_FROBENIUS_NORM) {
+      f = 1.0 - tr.x / cols;
+    } else if (variant == SQG_HILBERT_SCHMIDT_TEST) {
+      double d = 1.0 / cols;
+      f = 1.0 - d * d * (tr.x * tr.x + tr.y * tr.y);
+    } else {
+      double d = cols;
+      f = 1.0 - ((tr.x * tr.x + tr.y * tr.y) / d + 1) / (d + 1);
+    }
+    cost[b] = f;
+  }
+  if (!grad) return;
+  const int p = blockIdx.y * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double2 dt = make_double2(0.0, 0.0);
+  for (int t = 0; t < tiles; t++) {
+    double2 v = ws_gr[((long long)b * tiles + t) * P + p];
+    dt.x += v.x;
+    dt.y += v.y;
+  }
+  double gv;
+  if (variant == SQG_FROBENIUS_NORM) {
+    gv = (1.0 - dt.x / cols) - 1.0;
+  } else if (variant == SQG_HILBERT_SCHMIDT_TEST) {
+    double d = 1.0 / cols;
+    gv = -2.0 * d * d * tr.x * dt.x - 2.0 * d * d * tr.y * dt.y;
+  } else {
+    double d = cols;
+    gv = -2.0 / d / (d + 1) * tr.x * dt.x - 2.0 / d / (d + 1) * tr.y * dt.y;
+  }
+  grad[(long long)b * P + p] = gv;
+}
+
+// -------------------------------------------------------------------------------------
+// One pass over an HBM-resident matrix per gate (unfused application and the
+// combined-unitary parity API).  Thread = one amplitude pair x one column; consecutive
+// threads take consecutive columns, so every access is a coalesced 16-byte load.
+// deriv_k < 0: forward gate from gm; deriv_k >= 0: derivative kernel of parameter
+// deriv_k built from the stored sin/cos, with the pairs whose control bit is clear
+// zeroed (apply_kernel_to_input.cpp:93-97).
+// -------------------------------------------------------------------------------------
+__global__ void k_gate_hbm(double2* __restrict__ mtx, long long bstride, long long rstride, int cols, int logN,
+                           Gate gt, const GateMat* __restrict__ gmp, const double2* __restrict__ scp, int deriv_k,
+                           int nmat) {
+  const bool ctrl = gate_controlled(gt.type);
+  const bool deriv = deriv_k >= 0;
+  const int lognp = (!deriv && ctrl) ? logN - 2 : logN - 1;
+  const long long items = (long long)cols << lognp;
+  const int step = 1 << gt.target;
+  PairOp op;
+  double2 D[4];
+  if (deriv) {
+    deriv_kernel(gt.type, scp + gt.pstart, deriv_k, D);
+  } else {
+    op = make_op(gt.type, *gmp, ORIENT_FWD);
+  }
+  for (int b = blockIdx.y; b < nmat; b += gridDim.y) {
+    double2* base = mtx + (long long)b * bstride;
+    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items;
+         it += (long long)gridDim.x * blockDim.x) {
+      int p = (int)(it / cols);
+      int c = (int)(it - (long long)p * cols);
+      int i;
+      bool active = true;
+      if (!deriv) {
+        i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
+      } else {
+        i = pair_index1(p, gt.target);
+        active = !ctrl || ((i >> gt.control) & 1);
+      }
+      double2* px = base + (long long)i * rstride + c;
+      double2* py = base + (long long)(i + step) * rstride + c;
+      if (!active) {
+        *px = make_double2(0.0, 0.0);
+        *py = make_double2(0.0, 0.0);
+        continue;
+      }
+      double2 x = *px, y = *py;
+      if (!deriv) {
+        apply_op(op, x, y);
+      } else {
+        double2 nx, ny;
+        nx.x = D[0].x * x.x - D[0].y * x.y + D[1].x * y.x - D[1].y * y.y;
+        nx.y = D[0].x * x.y + D[0].y * x.x + D[1].x * y.y + D[1].y * y.x;
+        ny.x = D[2].x * x.x - D[2].y * x.y + D[3].x * y.x - D[3].y * y.y;
+        ny.y = D[2].x * x.y + D[2].y * x.x + D[3].x * y.y + D[3].y * y.x;
+        x = nx;
+        y = ny;
+      }
+      *px = x;
+      *py = y;
+    }
+  }
+}
+
+int hbm_blocks(long long items) { return (int)std::min<long long>((items + 255) / 256, 152LL * 16); }
+
+// ---- launch helpers ------------------------------------------------------------------
+struct TilePlan {
+  int TC, tiles, threads;
+  size_t smem;
+};
+
+int choose_threads(int tc, int N, bool grad) {
+  int items = tc * (N / 2);
+  int t = std::min(kMaxThreads, std::max(32, (items + 31) / 32 * 32));
+  (void)grad;
+  return t;
+}
+
+TilePlan plan_tiles(int N, int cols, bool grad) {
+  size_t per = (size_t)N * sizeof(double2) * (grad ? 2 : 1);
+  size_t budget = grad ? kSmemBudgetGrad : kSmemBudgetFwd;
+  int tc = (int)std::max<size_t>(1, budget / per);
+  // prefer powers of two, never more than the vectors available
+  int p2 = 1;
+  while (p2 * 2 <= tc) p2 *= 2;
+  tc = std::min(p2, cols);
+  TilePlan pl;
+  pl.TC = tc;
+  pl.tiles = (cols + tc - 1) / tc;
+  pl.threads = choose_threads(tc, N, grad);
+  size_t extra = grad ? (kMaxWarps * 8 + 8) * sizeof(double) + kMaxWarps * sizeof(double2)
+                      : kMaxWarps * sizeof(double2);
+  pl.smem = per * tc + extra;
+  return pl;
+}
+
+template <typename K>
+int set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
+  }
+  return SQG_OK;
+}
+
+struct PrepLayout {
+  size_t gm_off, sc_off, end;
+};
+PrepLayout prep_layout(const sqg_circuit* c, int B, size_t start) {
+  PrepLayout l;
+  l.gm_off = align_up(start, 256);
+  l.sc_off = align_up(l.gm_off + (size_t)B * std::max(c->L, 1) * sizeof(GateMat), 256);
+  l.end = align_up(l.sc_off + (size_t)B * std::max(c->P, 1) * sizeof(double2), 256);
+  return l;
+}
+
+struct EvalLayout {
+  PrepLayout prep;
+  size_t tr_off, gr_off, ck_off, end;
+  TilePlan plan;
+  int nck;
+};
+EvalLayout eval_layout(const sqg_circuit* c, int B, int cols, bool grad, int ckpt_interval) {
+  EvalLayout l;
+  l.prep = prep_layout(c, B, 0);
+  l.plan = plan_tiles(c->N, cols, grad);
+  l.tr_off = l.prep.end;
+  l.gr_off = align_up(l.tr_off + (size_t)B * l.plan.tiles * sizeof(double2), 256);
+  size_t gr_bytes = grad ? (size_t)B * l.plan.tiles * std::max(c->P, 1) * sizeof(double2) : 0;
+  l.ck_off = align_up(l.gr_off + gr_bytes, 256);
+  l.nck = 0;
+  if (grad && ckpt_interval > 0) l.nck = c->L / ckpt_interval;
+  size_t ck_bytes = (size_t)B * l.plan.tiles * l.nck * (size_t)l.plan.TC * c->N * sizeof(double2);
+  l.end = align_up(l.ck_off + ck_bytes, 256);
+  return l;
+}
+
+int launch_prep(const sqg_circuit* c, const double* theta, long long theta_stride, int B, GateMat* gm, double2* sc,
+                cudaStream_t st) {
+  if (c->L == 0) return SQG_OK;
+  dim3 grid((c->L + 127) / 128, B);
+  k_prep<<<grid, 128, 0, st>>>(c->d_gates, c->L, c->P, theta, theta_stride, B, gm, sc);
+  return cuda_status(cudaGetLastError(), "k_prep");
+}
+
+int check_circuit(const sqg_circuit* c) {
+  if (!c) return fail(SQG_ERR_INVALID_ARGUMENT, "null circuit handle");
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != c->device) return fail(SQG_ERR_INVALID_ARGUMENT, "circuit handle belongs to another device");
+  return SQG_OK;
+}
+
+}  // namespace
+
+// =====================================================================================
+// C ABI
+// =====================================================================================
+extern "C" {
+
+const char* sqg_status_string(int status) {
+  switch (status) {
+    case SQG_OK: return "ok";
+    case SQG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case SQG_ERR_UNSUPPORTED: return "unsupported configuration";
+    case SQG_ERR_WORKSPACE: return "workspace too small";
+    case SQG_ERR_CUDA: return "CUDA error";
+    case SQG_ERR_PARAMETER_COUNT: return "wrong number of parameters";
+    default: return "unknown status";
+  }
+}
+
+const char* sqg_last_error(void) { return g_last_error.c_str(); }
+
+int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_circuit** out) {
+  if (!out) return fail(SQG_ERR_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  if (qbit_num < 1 || qbit_num > 13) return fail(SQG_ERR_UNSUPPORTED, "qbit_num must be in 1..13");
+  if (gate_num < 0 || (gate_num > 0 && !gates)) return fail(SQG_ERR_INVALID_ARGUMENT, "bad gate list");
+  auto* c = new sqg_circuit();
+  c->n = qbit_num;
+  c->N = 1 << qbit_num;
+  c->L = gate_num;
+  int p = 0;
+  for (int i = 0; i < gate_num; i++) {
+    const sqg_gate& g = gates[i];
+    int t = g.type;
+    bool known = t == G_CZ || t == G_CNOT || t == G_U3 || t == G_RY || t == G_RX || t == G_RZ || t == G_CRY;
+    if (!known) {
+      delete c;
+      return fail(SQG_ERR_UNSUPPORTED, "gate " + std::to_string(i) + ": unsupported gate type " + std::to_string(t));
+    }
+    if (g.target < 0 || g.target >= qbit_num) {
+      delete c;
+      return fail(SQG_ERR_INVALID_ARGUMENT, "gate " + std::to_string(i) + ": target qubit out of range");
+    }
+    if (gate_controlled(t) && (g.control < 0 || g.control >= qbit_num || g.control == g.target)) {
+      delete c;
+      return fail(SQG_ERR_INVALID_ARGUMENT, "gate " + std::to_string(i) + ": bad control qubit");
+    }
+    if (g.param_start != p) {
+      delete c;
+      return fail(SQG_ERR_INVALID_ARGUMENT, "gate " + std::to_string(i) + ": parameters must be contiguous in gate order");
+    }
+    if (gate_controlled(t) && qbit_num < 2) {
+      delete c;
+      return fail(SQG_ERR_INVALID_ARGUMENT, "controlled gate needs two qubits");
+    }
+    Gate d{t, g.target, gate_controlled(t) ? g.control : -1, g.param_start};
+    c->h_gates.push_back(d);
+    p += gate_param_num(t);
+  }
+  c->P = p;
+  cudaGetDevice(&c->device);
+  if (gate_num > 0) {
+    cudaError_t e = cudaMalloc(&c->d_gates, sizeof(Gate) * gate_num);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_gates, c->h_gates.data(), sizeof(Gate) * gate_num, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      int st = cuda_status(e, "sqg_circuit_create");
+      cudaFree(c->d_gates);
+      delete c;
+      return st;
+    }
+  }
+  *out = c;
+  return SQG_OK;
+}
+
+int sqg_circuit_destroy(sqg_circuit* c) {
+  if (!c) return SQG_OK;
+  if (c->d_gates) cudaFree(c->d_gates);
+  delete c;
+  return SQG_OK;
+}
+
+int sqg_circuit_param_num(const sqg_circuit* c) { return c ? c->P : -1; }
+int sqg_circuit_qbit_num(const sqg_circuit* c) { return c ? c->n : -1; }
+int sqg_circuit_gate_num(const sqg_circuit* c) { return c ? c->L : -1; }
+
+size_t sqg_cost_grad_workspace_bytes(const sqg_circuit* c, int batch, int cols, int with_grad) {
+  if (!c || batch <= 0 || cols <= 0) return 0;
+  return eval_layout(c, batch, cols, with_grad != 0, 0).end;
+}
+
+size_t sqg_cost_grad_checkpoint_workspace_bytes(const sqg_circuit* c, int batch, int cols, int checkpoint_interval) {
+  if (!c || batch <= 0 || cols <= 0) return 0;
+  return eval_layout(c, batch, cols, true, checkpoint_interval).end;
+}
+
+int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* target, int cols,
+                  long long target_batch_stride, int trace_offset, int variant, double* cost, double* grad,
+                  int checkpoint_interval, void* workspace, size_t ws_bytes, void* stream) {
+  int st = check_circuit(c);
+  if (st) return st;
+  if (B <= 0 || B > 65535 || !target || !cost || cols <= 0)
+    return fail(SQG_ERR_INVALID_ARGUMENT, "bad batch (1..65535), target or output");
+  if (c->P > 0 && !theta) return fail(SQG_ERR_INVALID_ARGUMENT, "null parameter array");
+  if (cols > c->N) return fail(SQG_ERR_INVALID_ARGUMENT, "target has more columns than rows");
+  if (variant != SQG_FROBENIUS_NORM && variant != SQG_HILBERT_SCHMIDT_TEST && variant != SQG_INFIDELITY)
+    return fail(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
+  const int off = variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
+  if (off < 0 || off + cols > c->N) return fail(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
+  const bool with_grad = grad != nullptr && c->P > 0;
+  if (with_grad && c->n > 12) return fail(SQG_ERR_UNSUPPORTED, "gradient supports qbit_num <= 12");
+  if (checkpoint_interval < 0) return fail(SQG_ERR_INVALID_ARGUMENT, "negative checkpoint interval");
+  EvalLayout l = eval_layout(c, B, cols, with_grad, with_grad ? checkpoint_interval : 0);
+  if (!workspace || ws_bytes < l.end) return fail(SQG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(l.end));
+  cudaStream_t s = (cudaStream_t)stream;
+  char* ws = (char*)workspace;
+  GateMat* gm = (GateMat*)(ws + l.prep.gm_off);
+  double2* sc = (double2*)(ws + l.prep.sc_off);
+  double2* wtr = (double2*)(ws + l.tr_off);
+  double2* wgr = (double2*)(ws + l.gr_off);
+  if ((st = launch_prep(c, theta, c->P, B, gm, sc, s))) return st;
+  TileArgs a;
+  a.gates = c->d_gates;
+  a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N;
+  a.gm = gm; a.sc = sc;
+  a.mtx = (double2*)target;
+  a.bstride = target_batch_stride;
+  a.rstride = cols;
+  a.cstride = 1;
+  a.cols = cols;
+  a.TC = l.plan.TC;
+  a.tiles = l.plan.tiles;
+  a.trace_offset = off;
+  a.reverse_order = 0;
+  a.orient = ORIENT_FWD;
+  a.ws_tr = wtr;
+  a.ws_gr = wgr;
+  a.ckpt = l.nck > 0 ? (double2*)(ws + l.ck_off) : nullptr;
+  a.ckpt_interval = checkpoint_interval;
+  a.nck = l.nck;
+  dim3 grid(l.plan.tiles, B);
+  if (with_grad) {
+    if ((st = set_smem(k_tile_adjoint, l.plan.smem))) return st;
+    k_tile_adjoint<<<grid, l.plan.threads, l.plan.smem, s>>>(a);
+  } else {
+    if ((st = set_smem(k_tile_forward<false, true>, l.plan.smem))) return st;
+    k_tile_forward<false, true><<<grid, l.plan.threads, l.plan.smem, s>>>(a);
+  }
+  if ((st = cuda_status(cudaGetLastError(), "tile kernel"))) return st;
+  dim3 fgrid(B, with_grad ? (c->P + 127) / 128 : 1);
+  k_finish<<<fgrid, 128, 0, s>>>(wtr, wgr, l.plan.tiles, c->P, cols, variant, cost, with_grad ? grad : nullptr);
+  return cuda_status(cudaGetLastError(), "k_finish");
+}
+
+size_t sqg_apply_workspace_bytes(const sqg_circuit* c, int batch) {
+  if (!c || batch <= 0) return 0;
+  return prep_layout(c, batch, 0).end;
+}
+
+int sqg_apply(const sqg_circuit* c, const double* theta, int B, void* mtx, int cols, long long stride,
+              long long batch_stride, int fused, void* workspace, size_t ws_bytes, void* stream) {
+  int st = check_circuit(c);
+  if (st) return st;
+  if (B <= 0 || B > 65535 || !mtx || cols <= 0 || stride < cols)
+    return fail(SQG_ERR_INVALID_ARGUMENT, "bad matrix arguments");
+  if (c->P > 0 && !theta) return fail(SQG_ERR_INVALID_ARGUMENT, "null parameter array");
+  PrepLayout l = prep_layout(c, B, 0);
+  if (!workspace || ws_bytes < l.end) return fail(SQG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(l.end));
+  if (c->L == 0) return SQG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* ws = (char*)workspace;
+  GateMat* gm = (GateMat*)(ws + l.gm_off);
+  double2* sc = (double2*)(ws + l.sc_off);
+  if ((st = launch_prep(c, theta, c->P, B, gm, sc, s))) return st;
+  if (fused) {
+    TilePlan pl = plan_tiles(c->N, cols, false);
+    TileArgs a;
+    memset(&a, 0, sizeof(a));
+    a.gates = c->d_gates;
+    a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N;
+    a.gm = gm; a.sc = sc;
+    a.mtx = (double2*)mtx;
+    a.bstride = batch_stride;
+    a.rstride = stride;
+    a.cstride = 1;
+    a.cols = cols;
+    a.TC = pl.TC;
+    a.tiles = pl.tiles;
+    a.orient = ORIENT_FWD;
+    if ((st = set_smem(k_tile_forward<true, false>, pl.smem))) return st;
+    k_tile_forward<true, false><<<dim3(pl.tiles, B), pl.threads, pl.smem, s>>>(a);
+    return cuda_status(cudaGetLastError(), "k_tile_forward");
+  }
+  // unfused: one pass over the matrix per gate
+  for (int b = 0; b < B; b++) {
+    double2* base = (double2*)mtx + (long long)b * batch_stride;
+    for (int g = 0; g < c->L; g++) {
+      const Gate& gt = c->h_gates[g];
+      long long items = (long long)cols << (gate_controlled(gt.type) ? c->n - 2 : c->n - 1);
+      k_gate_hbm<<<dim3(hbm_blocks(items), 1), 256, 0, s>>>(base, 0, stride, cols, c->n, gt, gm + (long long)b * c->L + g,
+                                                          sc + (long long)b * c->P, -1, 1);
+    }
+  }
+  return cuda_status(cudaGetLastError(), "k_gate_hbm");
+}
+
+int sqg_apply_from_right(const sqg_circuit* c, const double* theta, void* mtx, int rows, long long stride,
+                         void* workspace, size_t ws_bytes, void* stream) {
+  int st = check_circuit(c);
+  if (st) return st;
+  if (!mtx || rows <= 0 || stride < c->N) return fail(SQG_ERR_INVALID_ARGUMENT, "bad matrix arguments");
+  if (c->P > 0 && !theta) return fail(SQG_ERR_INVALID_ARGUMENT, "null parameter array");
+  PrepLayout l = prep_layout(c, 1, 0);
+  if (!workspace || ws_bytes < l.end) return fail(SQG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(l.end));
+  if (c->L == 0) return SQG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* ws = (char*)workspace;
+  GateMat* gm = (GateMat*)(ws + l.gm_off);
+  double2* sc = (double2*)(ws + l.sc_off);
+  if ((st = launch_prep(c, theta, c->P, 1, gm, sc, s))) return st;
+  TilePlan pl = plan_tiles(c->N, rows, false);
+  TileArgs a;
+  memset(&a, 0, sizeof(a));
+  a.gates = c->d_gates;
+  a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N;
+  a.gm = gm; a.sc = sc;
+  a.mtx = (double2*)mtx;
+  a.bstride = 0;
+  a.rstride = stride;
+  a.cstride = 0;  // vectors are rows
+  a.cols = rows;
+  a.TC = pl.TC;
+  a.tiles = pl.tiles;
+  a.reverse_order = 1;
+  a.orient = ORIENT_TRANS;
+  if ((st = set_smem(k_tile_forward<true, false>, pl.smem))) return st;
+  k_tile_forward<true, false><<<dim3(pl.tiles, 1), pl.threads, pl.smem, s>>>(a);
+  return cuda_status(cudaGetLastError(), "k_tile_forward(right)");
+}
+
+int sqg_combined_unitary(const sqg_circuit* c, const double* theta, const void* target, int cols, void* out,
+                         void* workspace, size_t ws_bytes, void* stream) {
+  int st = check_circuit(c);
+  if (st) return st;
+  if (!target || !out || cols <= 0) return fail(SQG_ERR_INVALID_ARGUMENT, "bad matrix arguments");
+  if (c->P > 0 && !theta) return fail(SQG_ERR_INVALID_ARGUMENT, "null parameter array");
+  PrepLayout l = prep_layout(c, 1, 0);
+  if (!workspace || ws_bytes < l.end) return fail(SQG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(l.end));
+  cudaStream_t s = (cudaStream_t)stream;
+  char* ws = (char*)workspace;
+  GateMat* gm = (GateMat*)(ws + l.gm_off);
+  double2* sc = (double2*)(ws + l.sc_off);
+  const long long msz = (long long)c->N * cols;
+  double2* o = (double2*)out;
+  cudaError_t e = cudaMemcpyAsync(o, target, sizeof(double2) * msz, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_status(e, "sqg_combined_unitary");
+  if (c->L == 0) return SQG_OK;
+  if ((st = launch_prep(c, theta, c->P, 1, gm, sc, s))) return st;
+  // out[0] carries the forward state; derivative outputs out[1+k] are created from the
+  // state in front of their gate and then carried through the remaining gates
+  // (Gates_block::apply_derivate_to, Gates_block.cpp:1012-1150).
+  int created = 0;
+  for (int g = 0; g < c->L; g++) {
+    const Gate& gt = c->h_gates[g];
+    int np = gate_param_num(gt.type);
+    for (int k = 0; k < np; k++) {
+      double2* d = o + msz * (1 + gt.pstart + k);
+      e = cudaMemcpyAsync(d, o, sizeof(double2) * msz, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_status(e, "sqg_combined_unitary");
+      long long items = (long long)cols << (c->n - 1);
+      k_gate_hbm<<<dim3(hbm_blocks(items), 1), 256, 0, s>>>(d, 0, cols, cols, c->n, gt, gm + g, sc, k, 1);
+    }
+    // forward gate on out[0] and on the derivative outputs created before this gate
+    int nmat = 1 + created;
+    long long items = (long long)cols << (gate_controlled(gt.type) ? c->n - 2 : c->n - 1);
+    k_gate_hbm<<<dim3(hbm_blocks(items), std::min(nmat, 65535)), 256, 0, s>>>(o, msz, cols, cols, c->n, gt, gm + g, sc,
+                                                                             -1, nmat);
+    created += np;
+  }
+  return cuda_status(cudaGetLastError(), "sqg_combined_unitary");
+}
+
+}  // extern "C"

@@ -1,0 +1,223 @@
+"""Drop-in ``N_Qubit_Decomposition_custom`` on the GB300 engine.
+
+Mirrors squander.N_Qubit_Decomposition_custom
+(squander/decomposition/qgd_N_Qubit_Decompositions_Wrapper.cpp:347-400 and the method
+table at :3125-3250): the same constructor arguments, the same U^dagger target
+convention, parameter layout, cost-function variants and return shapes.  The cost and
+gradient run in the engine's CUDA kernels; the decomposition driver follows
+N_Qubit_Decomposition_custom::start_decomposition (src-cpp/decomposition/
+N_Qubit_Decomposition_custom.cpp:116-190) with BFGS for qbit_num <= 5 and ADAM above
+(:59-76).
+"""
+import math
+
+import numpy as np
+
+from . import _device as dev
+from .circuit import Circuit, combined_unitary_device
+from .evaluator import FROBENIUS_NORM, SUPPORTED_VARIANTS, CostEvaluator
+from .optim import adam, bfgs_powell
+
+_GUESS = {"zeros": "ZEROS", "random": "RANDOM", "close_to_zero": "CLOSE_TO_ZERO"}
+
+
+class N_Qubit_Decomposition_custom:
+    def __init__(self, Umtx, qbit_num=-1, initial_guess=None, config=None, accelerator_num=0):
+        U = np.asarray(Umtx)
+        if U.dtype == np.complex64:
+            raise NotImplementedError("the GB300 engine computes in FP64; pass a complex128 target")
+        if U.dtype != np.complex128 or U.ndim != 2:
+            raise TypeError("Umtx must be a 2-D complex128 array")
+        self.Umtx = np.ascontiguousarray(U)
+        if qbit_num == -1:
+            qbit_num = int(round(math.log2(self.Umtx.shape[0])))
+        if self.Umtx.shape[0] != (1 << qbit_num):
+            raise ValueError("the target must have 2**qbit_num rows")
+        self.qbit_num = int(qbit_num)
+        self.config = dict(config or {})
+        g = "random" if initial_guess is None else str(initial_guess).lower()
+        self.initial_guess = _GUESS.get(g, "RANDOM")
+        self.accelerator_num = accelerator_num
+        self.circuit = Circuit(self.qbit_num)
+        self.cost_variant = FROBENIUS_NORM
+        self.trace_offset = 0
+        self.optimization_tolerance = float(self.config.get("optimization_tolerance", 1e-7))
+        self.verbose = int(self.config.get("verbose", 0))
+        seed = self.config.get("random_seed")
+        self.rng = np.random.default_rng(None if seed is None else int(seed))
+        if self.qbit_num <= 5:
+            self.set_Optimizer("BFGS")
+            self.max_outer_iterations = 4
+        else:
+            self.set_Optimizer("ADAM")
+            self.max_outer_iterations = 1
+        self.optimized_parameters = np.zeros(0)
+        self.decomposition_error = None
+        self.num_iters = 0
+        self._evaluator = None
+
+    # ---- configuration -----------------------------------------------------------------
+    def set_Gate_Structure(self, gate_structure):
+        if not isinstance(gate_structure, Circuit):
+            raise TypeError("set_Gate_Structure expects a Circuit")
+        if gate_structure.qbit_num != self.qbit_num:
+            raise ValueError("the gate structure must span %d qubits" % self.qbit_num)
+        self.circuit = gate_structure
+        self._evaluator = None
+        return 0
+
+    def get_Circuit(self):
+        return self.circuit
+
+    def get_Parameter_Num(self):
+        return self.circuit.get_Parameter_Num()
+
+    def get_Qbit_Num(self):
+        return self.qbit_num
+
+    def set_Cost_Function_Variant(self, costfnc=0):
+        if int(costfnc) not in SUPPORTED_VARIANTS:
+            raise Exception("Optimization_Interface::optimization_problem: Cost function variant not implmented.")
+        self.cost_variant = int(costfnc)
+        self._evaluator = None
+
+    def set_Trace_Offset(self, trace_offset=0):
+        if trace_offset < 0 or trace_offset + self.Umtx.shape[1] > self.Umtx.shape[0]:
+            raise ValueError("trace offset out of range")
+        self.trace_offset = int(trace_offset)
+        self._evaluator = None
+
+    def get_Trace_Offset(self):
+        return self.trace_offset
+
+    def set_Optimizer(self, optimizer="BFGS"):
+        name = str(optimizer).upper()
+        if name not in ("BFGS", "ADAM"):
+            print("Wrong optimizer: %s. Using default: BFGS" % optimizer)
+            name = "BFGS"
+        self.optimizer = name
+        # Optimization_Interface::set_optimizer defaults (Optimization_Interface.cpp:1620-1697)
+        self.max_inner_iterations = 10000 if name == "BFGS" else 100000
+        return 0
+
+    def set_Optimization_Tolerance(self, tolerance):
+        self.optimization_tolerance = float(tolerance)
+
+    def set_Max_Iterations(self, max_iterations):
+        self.max_inner_iterations = int(max_iterations)
+
+    def set_Verbose(self, verbose):
+        self.verbose = int(verbose)
+
+    def set_Optimized_Parameters(self, new_params):
+        p = np.asarray(new_params, dtype=np.float64).reshape(-1)
+        if p.size != self.get_Parameter_Num():
+            raise ValueError("wrong number of parameters")
+        self.optimized_parameters = p.copy()
+        return 0
+
+    def get_Optimized_Parameters(self):
+        return self.optimized_parameters.copy()
+
+    def get_Decomposition_Error(self):
+        return self.decomposition_error
+
+    def get_Num_of_Iters(self):
+        return self.num_iters
+
+    # ---- cost / gradient -----------------------------------------------------------------
+    def evaluator(self):
+        if self._evaluator is None:
+            self._evaluator = CostEvaluator(self.circuit, self.Umtx, self.trace_offset, self.cost_variant)
+        return self._evaluator
+
+    def _params(self, parameters):
+        p = np.asarray(parameters)
+        if p.dtype == np.float32:
+            p = p.astype(np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1)
+        if p.size != self.get_Parameter_Num():
+            raise Exception("Optimization_Interface::optimization_problem: Wrong number of parameters.")
+        return p
+
+    def Optimization_Problem(self, parameters):
+        p = self._params(parameters)
+        cost, _ = self.evaluator().cost_grad(dev.to_device_real(p), with_grad=False)
+        self.num_iters += 1
+        return float(cost.item())
+
+    def Optimization_Problem_Combined(self, parameters):
+        p = self._params(parameters)
+        cost, grad = self.evaluator().cost_grad(dev.to_device_real(p), with_grad=True)
+        self.num_iters += p.size + 1
+        return float(cost.item()), grad.reshape(-1, 1).cpu().numpy()
+
+    def Optimization_Problem_Grad(self, parameters):
+        return self.Optimization_Problem_Combined(parameters)[1]
+
+    def Optimization_Problem_Batch(self, parameters):
+        p = np.asarray(parameters)
+        if p.dtype == np.float32:
+            p = p.astype(np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        if p.ndim != 2 or p.shape[1] != self.get_Parameter_Num():
+            raise Exception("Optimization_Interface::optimization_problem: Wrong number of parameters.")
+        cost, _ = self.evaluator().cost_grad(dev.to_device_real(p), with_grad=False)
+        return cost.reshape(-1, 1).cpu().numpy()
+
+    def Optimization_Problem_Combined_Unitary(self, parameters):
+        p = self._params(parameters)
+        out = combined_unitary_device(self.circuit.native(), dev.to_device_real(p), dev.to_device_complex(self.Umtx),
+                                      self.circuit._ws)
+        host = out.cpu().numpy()
+        return host[0], [host[k] for k in range(1, host.shape[0])]
+
+    def get_Matrix(self, parameters):
+        return self.circuit.get_Matrix(self._params(parameters))
+
+    # ---- decomposition driver --------------------------------------------------------------
+    def _fg(self, x):
+        cost, grad = self.evaluator().cost_grad(dev.to_device_real(x), with_grad=True)
+        return float(cost.item()), grad.reshape(-1).cpu().numpy()
+
+    def _initial(self, P):
+        if self.optimized_parameters.size == P:
+            return self.optimized_parameters.copy()
+        if self.initial_guess == "ZEROS":
+            return np.zeros(P)
+        x = self.rng.uniform(0.0, 2 * math.pi, P)
+        return x / 100 if self.initial_guess == "CLOSE_TO_ZERO" else x
+
+    def Start_Decomposition(self):
+        """Decomposition_Base::solve_optimization_problem for the custom structure
+        (Decomposition_Base.cpp:375-700 with optimization_block = all gates) with the
+        BFGS restarts of optimization_engines/BFGS.cpp:121-150."""
+        P = self.get_Parameter_Num()
+        if P == 0:
+            self.optimized_parameters = np.zeros(0)
+            self.decomposition_error = self.Optimization_Problem(np.zeros(0))
+            return 0
+        tol = float(self.config.get("optimization_tolerance", self.optimization_tolerance))
+        max_inner = int(self.config.get("max_inner_iterations_bfgs" if self.optimizer == "BFGS" else
+                                        "max_inner_iterations_adam", self.config.get("max_inner_iterations",
+                                                                                     self.max_inner_iterations)))
+        max_outer = int(self.config.get("max_outer_iterations", self.max_outer_iterations))
+        loops = int(self.config.get("max_iteration_loops", 3 if self.qbit_num == 2 else 1))
+        guess = self._initial(P)
+        best_x, best_f = guess.copy(), math.inf
+        for _outer in range(max_outer):
+            for _loop in range(loops):
+                if self.optimizer == "BFGS":
+                    f, calls = bfgs_powell(self._fg, guess, max_inner)
+                else:
+                    f, calls = adam(self._fg, guess, max_inner, tol=tol)
+                self.num_iters += calls
+                if f < best_f:
+                    best_f, best_x = f, guess.copy()
+                    guess += self.rng.uniform(0.0, 2 * math.pi, P) / 100
+            guess = best_x.copy()
+            if abs(best_f) < tol:
+                break
+        self.optimized_parameters = best_x
+        self.decomposition_error = self.Optimization_Problem(best_x)
+        return 0

@@ -1,0 +1,95 @@
+"""CPU-only tests: the C ABI library builds and exports every declared symbol, the
+host-side circuit bookkeeping, the host BFGS restatement, and loud failure without a GPU."""
+import ctypes
+import importlib
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(REPO, "include", "sqg.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sqg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_builds_and_exports_declared_symbols():
+    native = importlib.import_module("sequential-quantum-gate-decomposer_gb300._native")
+    path = native.build()
+    lib = ctypes.CDLL(path)
+    names = declared_functions()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(native.EXPORTED_SYMBOLS)
+
+
+def test_circuit_records_follow_reference_layout(sqg):
+    c = sqg.Circuit(3)
+    c.add_U3(0)
+    c.add_CNOT(1, 0)
+    c.add_RY(2)
+    c.add_CRY(0, 2)
+    sub = sqg.Circuit(3)
+    sub.add_RZ(1)
+    sub.add_CZ(2, 1)
+    c.add_Circuit(sub)
+    r = c.gate_records()
+    assert r.tolist() == [[7, 0, -1, 0], [5, 1, 0, 3], [8, 2, -1, 3], [14, 0, 2, 4], [10, 1, -1, 5], [4, 2, 1, 6]]
+    assert c.get_Parameter_Num() == 6
+    assert c.get_Gate_Nums() == {"U3": 1, "CNOT": 1, "RY": 1, "CRY": 1, "RZ": 1, "CZ": 1}
+    with pytest.raises(ValueError):
+        c.add_CNOT(1, 1)
+    with pytest.raises(ValueError):
+        c.add_U3(3)
+
+
+def test_workload_shapes(sqg):
+    wl = importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+    assert wl.cnot_u3_ansatz(4, 40).get_Parameter_Num() == 252
+    assert wl.cnot_u3_ansatz(8, 120).get_Parameter_Num() == 744
+    assert wl.cnot_u3_ansatz(8, 360).get_Parameter_Num() == 2184
+    assert wl.cnot_u3_ansatz(3, 14).get_Parameter_Num() == 93
+    rng = np.random.default_rng(0)
+    assert wl.cnot_u3_ansatz(10, 300, pairs="random", rng=rng).get_Parameter_Num() == 1830
+    U = wl.haar_unitary(16, np.random.default_rng(1))
+    assert np.allclose(U @ U.conj().T, np.eye(16), atol=1e-13)
+    assert wl.nearest_neighbour_pairs(3) == [(0, 1), (1, 0), (1, 2), (2, 1)]
+
+
+def test_host_bfgs_matches_oracle_driver(sqg):
+    """The engine's host BFGS restatement and the oracle's C restatement take the same
+    path on the same cost function (evaluated by the oracle here, on the CPU)."""
+    optim = importlib.import_module("sequential-quantum-gate-decomposer_gb300.optim")
+    wl = importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+    rng = np.random.default_rng(4)
+    c = wl.cnot_u3_ansatz(2, 3)
+    recs = c.gate_records()
+    P = c.get_Parameter_Num()
+    U = O.get_matrix(2, recs, rng.uniform(0, 2 * np.pi, P))
+    T = np.ascontiguousarray(U.conj().T)
+    x0 = rng.uniform(0, 2 * np.pi, P)
+    x_host = x0.copy()
+    f_host, calls = optim.bfgs_powell(lambda x: O.cost_grad(2, recs, x, T), x_host, 10000)
+    x_or, f_or, calls_or = O.decompose(2, recs, T[None], x0[None], tolerance=0.0, max_outer=1, iteration_loops=1)
+    assert calls == calls_or[0]
+    assert f_host == pytest.approx(f_or[0], abs=1e-13)
+    assert np.allclose(x_host, x_or[0], atol=1e-9)
+
+
+def test_engine_fails_loudly_without_gpu(sqg):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    c = sqg.Circuit(2)
+    c.add_U3(0)
+    with pytest.raises(Exception):
+        c.get_Matrix(np.zeros(3))
+    with pytest.raises(Exception):
+        sqg.CostEvaluator(c, np.eye(4, dtype=np.complex128))
