@@ -1,0 +1,413 @@
+#!/usr/bin/env python3
+"""Benchmark of the decomposition hot path on one GB300.
+
+Headline metric: 3-qubit decompositions per second reaching FROBENIUS_NORM cost < 1e-8.
+Workload: 4096 held-out 3-qubit targets (half Haar-random 8x8, half products of random
+CNOT+U3 circuits with 1..14 CNOTs; seeded synthetic data), fixed 14-block
+nearest-neighbour CNOT+U3 ansatz (93 parameters), batched 4096-wide on the device.  One
+step = one batched decomposition pass over all 4096 targets from fresh random starts.
+Secondary lines inside the same JSON object: gate application at n=12 (2000-gate random
+circuit, batch of 4 parameter vectors, fused vs unfused, HBM GB/s) and the batched
+cost+gradient evaluation at n=8 (B=1024, 360 blocks).
+
+--impl reference times the reference algorithm on the host cores instead (the oracle's
+C restatement of SQUANDER's BFGS decomposition; the reference itself is not buildable
+here).
+"""
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+PKG = "sequential-quantum-gate-decomposer_gb300"
+
+METRIC = "3q decompositions/s to cost<1e-8"
+UNIT = "decompositions/s"
+N_TARGETS = 4096
+ANSATZ_BLOCKS = 14
+TOL = 1e-8
+MAX_CALLS = 2000      # cost+gradient evaluations per BFGS run
+MAX_OUTER = 4         # restarts (N_Qubit_Decomposition_custom uses 4 outer iterations)
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# FP64 FMA pipe peak measured on this machine's GB300 with a dependent-free DFMA loop
+# (profiles/fp64_peak_probe.md): 1.20 TFLOP/s counting an FMA as 2 flops.
+FP64_PEAK_TFLOPS = 1.20
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", "bench_clocks.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(sqg, wl, orc_matrix=None, seed=1234):
+    rng = np.random.default_rng(seed)
+    ansatz = wl.cnot_u3_ansatz(3, ANSATZ_BLOCKS)
+    if orc_matrix is None:
+        def orc_matrix(circ, theta):
+            return circ.get_Matrix(theta)
+    U = wl.three_qubit_targets(N_TARGETS, rng, orc_matrix)
+    targets = np.ascontiguousarray(np.conj(np.transpose(U, (0, 2, 1))))
+    return ansatz, targets
+
+
+def flush_l2(buf):
+    buf.add_(1)
+
+
+def fp64_ops_per_eval(circuit_records, N, cols):
+    """FP64 instructions of one cost+gradient evaluation in the tile kernels (update
+    rules of gates.cuh): forward per pair U3 14, RX/RY/RZ 8, CRY 8 on the controlled
+    quarter of rows... reverse per pair: uncompute + R accumulation (16) + co-state."""
+    ops = 0
+    for t, tg, c, ps in circuit_records:
+        pairs_all = (N // 2) * cols
+        pairs_ctl = (N // 4) * cols
+        if t == 7:
+            fwd, pairs = 14, pairs_all
+        elif t in (8, 9, 10):
+            fwd, pairs = 8, pairs_all
+        elif t == 14:
+            fwd, pairs = 8, pairs_ctl
+        else:
+            continue
+        ops += pairs * (fwd + fwd + 16 + fwd)
+    return ops
+
+
+def bench_ours(args):
+    import torch
+
+    sqg = importlib.import_module(PKG)
+    wl = importlib.import_module(PKG + ".workloads")
+    torch.cuda.set_device(0)
+    ansatz, targets = make_workload(sqg, wl)
+    P = ansatz.get_Parameter_Num()
+    dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=MAX_CALLS, max_outer=MAX_OUTER)
+    tdev = torch.from_numpy(targets).cuda()
+    rng = np.random.default_rng(99)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    stream = torch.cuda.current_stream()
+
+    def step(seed, host=False):
+        x0 = rng.uniform(0, 2 * np.pi, (N_TARGETS, P))
+        if host:
+            return dec.run(targets, x0, seed=seed)
+        return dec.run(tdev, torch.from_numpy(x0).cuda(), seed=seed)
+
+    for w in range(args.warmup):
+        step(w)
+    torch.cuda.synchronize()
+    # device-resident inputs: x0 generated on the host beforehand is part of the input
+    x0s = [torch.from_numpy(rng.uniform(0, 2 * np.pi, (N_TARGETS, P))).cuda() for _ in range(args.steps)]
+    clocks = Clocks()
+    clocks.start()
+    times, solved, calls_tot = [], 0, 0
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush_l2(flush)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        x, cost, calls = dec.run(tdev, x0s[k], seed=1000 + k)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        c = cost.cpu().numpy()
+        solved += int((c < TOL).sum())
+        calls_tot += int(calls.cpu().numpy().astype(np.int64).sum())
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_total = sum(times)
+    value = solved / t_total
+    # end to end: host targets and start points in, host results out
+    e2e_times, e2e_solved = [], 0
+    for k in range(max(1, min(args.steps, 3))):
+        x0 = rng.uniform(0, 2 * np.pi, (N_TARGETS, P))
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x, cost, calls = dec.run(targets, x0, seed=2000 + k)
+        xh = x.cpu().numpy()
+        ch = cost.cpu().numpy()
+        e2e_times.append(time.perf_counter() - t0)
+        e2e_solved += int((ch < TOL).sum())
+    e2e_value = e2e_solved / sum(e2e_times)
+    h2d = targets.nbytes + N_TARGETS * P * 8
+    d2h = N_TARGETS * P * 8 + N_TARGETS * 8
+    # roofline of the decomposition kernel (FP64 pipe): algorithmic FP64 ops from the
+    # evaluations actually performed; BFGS linear algebra adds about 6 P^2 per iteration
+    ops_eval = fp64_ops_per_eval(ansatz.gate_records(), 8, 8)
+    achieved_tflops = 2.0 * ops_eval * calls_tot / t_total / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Haar + random-circuit 3-qubit targets)",
+        "config": {"workload": "config 4 plain path: 4096 3-qubit targets, 14-block NN CNOT+U3 ansatz (93 params), "
+                               "BFGS random start, batched 4096-wide",
+                   "targets": N_TARGETS, "params": P, "tolerance": TOL, "max_calls_per_bfgs": MAX_CALLS,
+                   "restarts": MAX_OUTER, "init": "random U[0,2pi)", "l2": "flushed between steps (256 MB write)"},
+        "solved_fraction": solved / (N_TARGETS * args.steps),
+        "evaluations_per_step": calls_tot / args.steps,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "frac": achieved_tflops / FP64_PEAK_TFLOPS, "traffic": None,
+                     "note": "k_decompose is FP64-pipe bound (GB300 FP64 = 1.2 TFLOP/s measured); counts only the "
+                             "cost+gradient FP64 ops, not the BFGS linear algebra"},
+    }
+    if clk:
+        line["clocks"] = clk
+    if not args.skip_secondary:
+        line["gate_apply_n12"] = bench_gate_apply(sqg, wl, torch)
+        line["cost_grad_n8"] = bench_cost_grad(sqg, wl, torch)
+    if not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(sqg, wl, ansatz, targets, P, budget_s=args.cpu_seconds)
+    return line
+
+
+def bench_gate_apply(sqg, wl, torch):
+    """n=12, 2000 random gates of U3/RY/CNOT/CZ/CRY, batch of 4 parameter vectors."""
+    hbm, src = peaks()
+    n, L, B = 12, 2000, 4
+    rng = np.random.default_rng(5)
+    c = wl.random_gate_circuit(n, L, rng)
+    P = c.get_Parameter_Num()
+    N = 1 << n
+    th = torch.from_numpy(rng.uniform(0, 2 * np.pi, (B, P))).cuda()
+    m = torch.empty((B, N, N), dtype=torch.complex128, device="cuda")
+    m.real.normal_()
+    recs = c.gate_records()
+    frac = {7: 1.0, 8: 1.0, 9: 1.0, 10: 1.0, 5: 0.5, 14: 0.5, 4: 0.25}
+    alg_bytes = sum(32.0 * N * N * frac[int(t)] for t, _, _, _ in recs)  # per parameter vector
+    res = {}
+    for fused in (True, False):
+        c.apply_to_device(th, m, fused=fused)  # warm-up
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c.apply_to_device(th, m, fused=fused)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        key = "fused" if fused else "unfused"
+        res[key] = {"seconds": t, "algorithmic_GBps": B * alg_bytes / t / 1e9}
+        if fused:
+            res[key]["hbm_pass_GBps"] = B * 32.0 * N * N / t / 1e9
+    fwd_ops = 0
+    for t_, tg, ctl, ps in recs:
+        t_ = int(t_)
+        if t_ == 7:
+            fwd_ops += 14 * (N // 2) * N
+        elif t_ in (8, 9, 10):
+            fwd_ops += 8 * (N // 2) * N
+        elif t_ == 14:
+            fwd_ops += 8 * (N // 4) * N
+    res["fused"]["fp64_tflops"] = 2.0 * B * fwd_ops / res["fused"]["seconds"] / 1e12
+    res["fused"]["fp64_frac"] = res["fused"]["fp64_tflops"] / FP64_PEAK_TFLOPS
+    res["unfused"]["hbm_frac"] = res["unfused"]["algorithmic_GBps"] / hbm
+    res["unfused"]["fp64_tflops"] = 2.0 * B * fwd_ops / res["unfused"]["seconds"] / 1e12
+    res["peak_hbm_GBps"] = hbm
+    res["peak_source"] = src
+    res["config"] = "n=12 (4096x4096 complex128), 2000 random gates U3/RY/CNOT/CZ/CRY, batch 4"
+    del m
+    return res
+
+
+def bench_cost_grad(sqg, wl, torch):
+    """n=8 target from a 360-block ansatz at seeded angles, B=1024 parameter vectors."""
+    n, blocks, B = 8, 360, 1024
+    rng = np.random.default_rng(6)
+    c = wl.cnot_u3_ansatz(n, blocks)
+    P = c.get_Parameter_Num()
+    U = c.get_Matrix(rng.uniform(0, 2 * np.pi, P))
+    ev = sqg.CostEvaluator(c, np.ascontiguousarray(U.conj().T))
+    th = torch.from_numpy(rng.uniform(0, 2 * np.pi, (B, P))).cuda()
+    ev.cost_grad(th[:8])
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ev.cost_grad(th)
+    e1.record()
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    ops = fp64_ops_per_eval(c.gate_records(), 1 << n, 1 << n) + 0
+    return {"config": "n=8, 360 blocks (P=2184), B=1024, cost+adjoint gradient", "seconds": t,
+            "evals_per_s": B / t, "fp64_tflops": 2.0 * ops * B / t / 1e12,
+            "fp64_frac": 2.0 * ops * B / t / 1e12 / FP64_PEAK_TFLOPS}
+
+
+def cpu_baseline(sqg, wl, ansatz, targets, P, budget_s=20.0):
+    from oracle import oracle as orc
+
+    threads = os.cpu_count() or 1
+    recs = ansatz.gate_records()
+    rng = np.random.default_rng(77)
+    # bounded sample: grow the number of targets until about budget_s of CPU work
+    n = threads
+    t0 = time.perf_counter()
+    solved, done = 0, 0
+    while True:
+        idx = np.arange(done, done + n) % N_TARGETS
+        x0 = rng.uniform(0, 2 * np.pi, (n, P))
+        _, cost, _ = orc.decompose(3, recs, targets[idx], x0, tolerance=TOL, max_inner=MAX_CALLS,
+                                   max_outer=MAX_OUTER, nthreads=threads, seed=int(rng.integers(1 << 31)))
+        solved += int((cost < TOL).sum())
+        done += n
+        if time.perf_counter() - t0 > budget_s or done >= N_TARGETS:
+            break
+    t = time.perf_counter() - t0
+    return {"value": solved / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of the 4096 targets, same ansatz, tolerance and BFGS budgets, oracle C restatement of "
+                      "SQUANDER's BFGS decomposition with %d threads (%.1f s)" % (done, threads, t),
+            "solved_fraction": solved / done}
+
+
+def bench_reference(args):
+    """Reference arm: the reference algorithm on the host cores (oracle C restatement)."""
+    from oracle import oracle as orc
+
+    sqg = importlib.import_module(PKG)
+    wl = importlib.import_module(PKG + ".workloads")
+    ansatz_rec = None
+
+    def mat(circ, theta):
+        return orc.get_matrix(circ.qbit_num, circ.gate_records(), theta)
+
+    ansatz, targets = make_workload(sqg, wl, orc_matrix=mat)
+    P = ansatz.get_Parameter_Num()
+    recs = ansatz.gate_records()
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(77)
+    per_step = max(threads, int(args.ref_targets))
+
+    def step(k):
+        idx = (np.arange(per_step) + k * per_step) % N_TARGETS
+        x0 = rng.uniform(0, 2 * np.pi, (per_step, P))
+        t0 = time.perf_counter()
+        _, cost, _ = orc.decompose(3, recs, targets[idx], x0, tolerance=TOL, max_inner=MAX_CALLS,
+                                   max_outer=MAX_OUTER, nthreads=threads, seed=k)
+        return time.perf_counter() - t0, int((cost < TOL).sum())
+
+    for w in range(args.warmup):
+        step(100 + w) if per_step <= 64 else None
+    times, solved = [], 0
+    for k in range(args.steps):
+        t, s = step(k)
+        times.append(t)
+        solved += s
+    value = solved / sum(times)
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "config 4 plain path, bounded sample of %d targets per step" % per_step,
+                       "params": P, "tolerance": TOL},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d targets per step" % per_step},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-secondary", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--ref-targets", type=int, default=32)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(bench_reference(args)))
+        return
+    if world > 1:
+        # replicas: every rank decomposes its own 4096 targets; rank 0 reports the sum
+        import torch
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        args.skip_secondary = True
+        args.skip_cpu = rank != 0
+        line = bench_ours(args)
+        t = torch.tensor([line["ms_per_step"]], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        if rank == 0:
+            line["ms_per_step"] = float(t.item())
+            line["value"] = line["value"] * world * 0 + (line["solved_fraction"] * N_TARGETS * world) / (
+                line["ms_per_step"] / 1e3)
+            line["n_gpus"] = world
+            print(json.dumps(line))
+        dist.destroy_process_group()
+        return
+    print(json.dumps(bench_ours(args)))
+
+
+if __name__ == "__main__":
+    main()

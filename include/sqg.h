@@ -125,6 +125,26 @@ int sqg_apply_from_right(const sqg_circuit* circuit, const double* theta_dev, vo
 int sqg_combined_unitary(const sqg_circuit* circuit, const double* theta_dev, const void* target_dev, int cols,
                          void* out_dev, void* workspace_dev, size_t workspace_bytes, void* stream);
 
+/* Batched decomposition of `batch` small targets (qbit_num <= 5), one complete BFGS
+ * decomposition per CTA, entirely on the device.
+ *   targets_dev  batch x rows x cols complex128 (each U^dagger);
+ *   x_dev        batch x P doubles: start points in, best parameters out;
+ *   cost_dev     batch doubles out (best cost);  calls_dev  batch ints out (cost+gradient
+ *                evaluations used).
+ * Each instance runs up to max_outer outer iterations of iteration_loops BFGS runs of at
+ * most max_calls evaluations, perturbing the best point by U[0, 2 pi)/100 after an
+ * improvement, and stops once the best cost is below `tolerance`; with
+ * stop_at_tolerance != 0 a run also stops at the first evaluation below it.  Replaces
+ * N_Qubit_Decomposition_custom::start_decomposition with the BFGS optimizer
+ * (src-cpp/decomposition/N_Qubit_Decomposition_custom.cpp:116-190,
+ * src-cpp/optimization_engines/BFGS.cpp:42-152, src-cpp/common/BFGS_Powell.cpp:70-396).
+ * The workspace holds the per-instance BFGS matrices when they do not fit on chip. */
+size_t sqg_decompose_workspace_bytes(const sqg_circuit* circuit, int batch, int cols);
+int sqg_decompose_batched(const sqg_circuit* circuit, const void* targets_dev, int cols, int batch, int trace_offset,
+                          int cost_variant, double* x_dev, double* cost_dev, int* calls_dev, double tolerance,
+                          int max_calls, int max_outer, int iteration_loops, int stop_at_tolerance,
+                          unsigned long long seed, void* workspace_dev, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,7 @@ also registers itself under the alias ``sqg_gb300``.
 import sys as _sys
 
 from ._native import SQGError, build
+from .batched import BatchedDecomposer
 from .circuit import CNOT, CRY, CZ, RX, RY, RZ, U3, Circuit
 from .decomposition import N_Qubit_Decomposition_custom
 from .evaluator import (FROBENIUS_NORM, HILBERT_SCHMIDT_TEST, INFIDELITY, CircuitCost, CostEvaluator,
@@ -20,6 +21,6 @@ from .evaluator import (FROBENIUS_NORM, HILBERT_SCHMIDT_TEST, INFIDELITY, Circui
 
 _sys.modules.setdefault("sqg_gb300", _sys.modules[__name__])
 
-__all__ = ["Circuit", "N_Qubit_Decomposition_custom", "CostEvaluator", "CircuitCost", "circuit_cost", "SQGError",
+__all__ = ["Circuit", "BatchedDecomposer", "N_Qubit_Decomposition_custom", "CostEvaluator", "CircuitCost", "circuit_cost", "SQGError",
            "build", "FROBENIUS_NORM", "HILBERT_SCHMIDT_TEST", "INFIDELITY", "U3", "RX", "RY", "RZ", "CNOT", "CZ",
            "CRY"]

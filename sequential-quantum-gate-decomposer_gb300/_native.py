@@ -17,7 +17,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 LIB_PATH = os.path.join(PKG_DIR, "libsqg.so")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-CU_SOURCES = ["engine.cu"]
+CU_SOURCES = ["engine.cu", "decompose.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -106,6 +106,10 @@ def _declare(lib):
     lib.sqg_apply.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_ll, c_int, vp, c_sz, vp]
     lib.sqg_apply_from_right.argtypes = [vp, vp, vp, c_int, c_ll, vp, c_sz, vp]
     lib.sqg_combined_unitary.argtypes = [vp, vp, vp, c_int, vp, vp, c_sz, vp]
+    lib.sqg_decompose_workspace_bytes.restype = c_sz
+    lib.sqg_decompose_workspace_bytes.argtypes = [vp, c_int, c_int]
+    lib.sqg_decompose_batched.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, ctypes.c_double, c_int,
+                                          c_int, c_int, c_int, ctypes.c_ulonglong, vp, c_sz, vp]
 
 
 def lib():
@@ -132,5 +136,5 @@ EXPORTED_SYMBOLS = [
     "sqg_status_string", "sqg_last_error", "sqg_circuit_create", "sqg_circuit_destroy", "sqg_circuit_param_num",
     "sqg_circuit_qbit_num", "sqg_circuit_gate_num", "sqg_cost_grad_workspace_bytes",
     "sqg_cost_grad_checkpoint_workspace_bytes", "sqg_cost_grad", "sqg_apply_workspace_bytes", "sqg_apply",
-    "sqg_apply_from_right", "sqg_combined_unitary",
+    "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched",
 ]

@@ -1,0 +1,59 @@
+"""Batched decompositions on the device (one BFGS decomposition per CTA, one launch).
+
+This is the throughput form of SQUANDER's ``N_Qubit_Decomposition_custom`` with the
+BFGS optimizer (src-cpp/decomposition/N_Qubit_Decomposition_custom.cpp:116-190): every
+target of the batch is decomposed with the same gate structure, each from its own start
+point, without a host round trip per iteration.
+"""
+import numpy as np
+
+from . import _device as dev
+from . import _native
+from .circuit import Circuit
+
+
+class BatchedDecomposer:
+    """Decomposes batches of targets (each given as U^dagger) with one gate structure."""
+
+    def __init__(self, circuit, tolerance=1e-8, max_calls=10000, max_outer=4, iteration_loops=1,
+                 stop_at_tolerance=True, trace_offset=0, cost_variant=0):
+        dev.require_cuda()
+        if not isinstance(circuit, Circuit):
+            raise TypeError("circuit must be a Circuit")
+        self.circuit = circuit
+        self.native = circuit.native()
+        self.tolerance = float(tolerance)
+        self.max_calls = int(max_calls)
+        self.max_outer = int(max_outer)
+        self.iteration_loops = int(iteration_loops)
+        self.stop_at_tolerance = bool(stop_at_tolerance)
+        self.trace_offset = int(trace_offset)
+        self.cost_variant = int(cost_variant)
+        self._ws = dev.Workspace()
+
+    def run(self, targets_udag, x0, seed=0, stream=None):
+        """targets_udag: (B, rows, cols) complex128; x0: (B, P) float64 (host or device).
+        Returns CUDA tensors (x (B, P), cost (B,), calls (B,) int32); asynchronous."""
+        t = dev.to_device_complex(targets_udag)
+        if t.dim() != 3 or t.shape[1] != (1 << self.native.qbit_num):
+            raise ValueError("targets must be (B, 2**qbit_num, cols)")
+        B, _, cols = t.shape
+        x = dev.to_device_real(x0).clone()
+        if x.shape != (B, self.native.param_num):
+            raise ValueError("x0 must be (B, %d)" % self.native.param_num)
+        cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
+        calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
+        lib = _native.lib()
+        ws = self._ws.get(lib.sqg_decompose_workspace_bytes(self.native.handle, B, cols))
+        _native.check(lib.sqg_decompose_batched(
+            self.native.handle, dev.ptr(t), cols, B, self.trace_offset, self.cost_variant, dev.ptr(x), dev.ptr(cost),
+            dev.ptr(calls), self.tolerance, self.max_calls, self.max_outer, self.iteration_loops,
+            1 if self.stop_at_tolerance else 0, int(seed) & 0xFFFFFFFFFFFFFFFF, dev.ptr(ws), ws.numel(),
+            dev.stream_ptr(stream)), "sqg_decompose_batched")
+        self._keep = t  # keep the target buffer alive until the caller synchronises
+        return x, cost, calls
+
+
+def random_start(B, P, rng):
+    """RANDOM initial guess of Decomposition_Base (U[0, 2 pi), Decomposition_Base.cpp:415-436)."""
+    return rng.uniform(0.0, 2 * np.pi, (B, P))

@@ -1,0 +1,416 @@
+// Batched decomposition: one CTA runs one complete decomposition (BFGS with Powell's
+// Z-matrix update, its line search and the restart loop) of one small target, with the
+// cost and adjoint gradient evaluated in the CTA's shared memory.  A single launch
+// decomposes the whole batch; no host round trip happens per iteration.
+//
+// Algorithm restated from the reference:
+//   src-cpp/common/BFGS_Powell.cpp:70-192 (Optimize), :202-396 (BFGS_iteration),
+//   :407-446 (get_search_direction); src-cpp/common/grad_descend.cpp:127-273 (line
+//   search), :399-425 (maximal step); restarts: optimization_engines/BFGS.cpp:121-150 and
+//   Decomposition_Base.cpp:375-700 (outer loop, tolerance test :742-752).
+// The Givens sweep of the Z update is evaluated in parallel from suffix sums of squares
+// of Z^T g instead of the sequential hypot chain (same rotations up to rounding).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "../../include/sqg.h"
+#include "gates.cuh"
+#include "handle.h"
+#include "tile.cuh"
+
+using namespace sqg;
+
+
+namespace {
+
+constexpr int kDecThreads = 128;
+constexpr double kNumPrecision = 1.42e-14;  // grad_descend.cpp:37
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+struct DecArgs {
+  const Gate* gates;
+  int L, P, n, N, cols, trace_offset, variant;
+  const double2* targets;
+  long long tstride;
+  double* x;
+  double* cost;
+  int* calls;
+  int B;
+  double tol;
+  int max_calls, max_outer, loops, early_stop;
+  unsigned long long seed;
+  double* zglob;
+  int z_in_smem;
+};
+
+struct Sh {
+  double2 *psi, *lam, *sc, *T;
+  GateMat* gm;
+  double *x, *g, *d, *x0, *g0, *gbest, *ztg, *delta, *gamma, *gtz, *nz, *bestx, *guess, *S;
+  double *Z, *redd, *tot, *scratch;
+};
+
+__device__ __forceinline__ double u01(unsigned long long k) {
+  unsigned long long z = k + 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__device__ double dot(const double* a, const double* b, int P, double* scratch) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) s = fma(a[i], b[i], s);
+  return block_allsum(s, scratch);
+}
+
+// Cost and gradient of parameter vector xv (smem) for instance b; gradient into gv.
+__device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, double* gv, int b) {
+  const int N = a.N, cols = a.cols, off = a.trace_offset;
+  build_gate_mats(a.gates, a.L, xv, sh.gm, sh.sc);
+  const double2* T = a.targets + (long long)b * a.tstride;
+  for (int e = threadIdx.x; e < N * cols; e += blockDim.x) {
+    int r = e / cols, c = e - r * cols;
+    sh.psi[c * N + r] = T[e];
+    sh.lam[c * N + r] = make_double2(r == c + off ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int g = 0; g < a.L; g++) {
+    Gate gt = a.gates[g];
+    tile_apply(sh.psi, N, a.n, cols, gt, make_op(gt.type, sh.gm[g], ORIENT_FWD));
+    __syncthreads();
+  }
+  double2 tr = tile_trace(sh.psi, N, cols, 0, off, sh.scratch);
+  double2* Tp = sh.T;
+  adjoint_sweep(sh.psi, sh.lam, N, a.n, cols, a.gates, sh.gm, sh.sc, a.L, sh.redd, sh.tot,
+                [&](int p, double2 v) { Tp[p] = v; }, [](int) {});
+  __syncthreads();
+  double f;
+  const double dc = cols;
+  if (a.variant == SQG_FROBENIUS_NORM) {
+    f = 1.0 - tr.x / dc;
+  } else if (a.variant == SQG_HILBERT_SCHMIDT_TEST) {
+    double d = 1.0 / dc;
+    f = 1.0 - d * d * (tr.x * tr.x + tr.y * tr.y);
+  } else {
+    f = 1.0 - ((tr.x * tr.x + tr.y * tr.y) / dc + 1) / (dc + 1);
+  }
+  for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
+    double2 t = Tp[p];
+    double gvv;
+    if (a.variant == SQG_FROBENIUS_NORM) {
+      gvv = (1.0 - t.x / dc) - 1.0;
+    } else if (a.variant == SQG_HILBERT_SCHMIDT_TEST) {
+      double d = 1.0 / dc;
+      gvv = -2.0 * d * d * tr.x * t.x - 2.0 * d * d * tr.y * t.y;
+    } else {
+      gvv = -2.0 / dc / (dc + 1) * tr.x * t.x - 2.0 / dc / (dc + 1) * tr.y * t.y;
+    }
+    gv[p] = gvv;
+  }
+  __syncthreads();
+  return f;
+}
+
+// BFGS_Powell::BFGS_iteration (BFGS_Powell.cpp:202-396); returns the updated norm_Z.
+__device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z) {
+  const int P = a.P;
+  double* Z = sh.Z;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    sh.delta[i] = sh.x[i] - sh.x0[i];
+    sh.gamma[i] = sh.g[i] - sh.g0[i];
+  }
+  __syncthreads();
+  double norm_delta = dot(sh.delta, sh.delta, P, sh.scratch);
+  double tmp = dot(sh.g0, sh.delta, P, sh.scratch);
+  double dtg = dot(sh.gamma, sh.delta, P, sh.scratch);
+  if (dtg < fabs(tmp) * 0.1) return norm_Z;
+  dtg = fmax(kNumPrecision, dtg);
+  // Givens sweep from suffix sums of squares of ztg: the rotation at column col (pairing
+  // col-1 and col) has a = |ztg[col-1:]|, cv = ztg[col-1]/a, sv = r/a with r = |ztg[col:]|,
+  // or r = ztg[col] itself when everything after col is zero.
+  for (int k = threadIdx.x; k < P; k += blockDim.x) {
+    double s = 0.0;
+    for (int i = P - 1; i >= k; i--) s = fma(sh.ztg[i], sh.ztg[i], s);
+    sh.S[k] = s;
+  }
+  // last nonzero index of ztg
+  double lastnz = -1.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x)
+    if (sh.ztg[i] != 0.0) lastnz = fmax(lastnz, (double)i);
+  lastnz = -block_allmin(-lastnz, sh.scratch);
+  const int m = (int)lastnz;
+  __syncthreads();
+  for (int col = threadIdx.x + 1; col < P; col += blockDim.x) {
+    if (col <= m) {
+      double av = sqrt(sh.ztg[col - 1] * sh.ztg[col - 1] + sh.S[col]);
+      double r = col == m ? sh.ztg[col] : sqrt(sh.S[col]);
+      sh.gtz[col] = sh.ztg[col - 1] / av;  // cos
+      sh.nz[col] = r / av;                 // sin
+    }
+  }
+  __syncthreads();
+  const int top = min(m, P - 1);
+  for (int r = threadIdx.x; r < P; r += blockDim.x) {
+    double* row = Z + (long long)r * P;
+    for (int col = top; col >= 1; col--) {
+      double cv = sh.gtz[col], sv = sh.nz[col];
+      double zc = row[col - 1], zn = row[col];
+      row[col] = cv * zn - sv * zc;
+      row[col - 1] = cv * zc + sv * zn;
+    }
+  }
+  if (norm_Z < 0.0) {
+    norm_Z = norm_delta / dtg;
+  } else {
+    double t = sqrt(norm_Z * norm_delta / dtg);
+    norm_Z = fmin(norm_Z, t);
+    norm_Z = fmax(norm_Z, t * 0.1);
+  }
+  const double sd = sqrt(dtg);
+  __syncthreads();
+  for (int r = threadIdx.x; r < P; r += blockDim.x)
+    Z[(long long)r * P] = fabs(sh.delta[r]) > kNumPrecision ? sh.delta[r] / sd : 0.0;
+  __syncthreads();
+  for (int c = threadIdx.x + 1; c < P; c += blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < P; r++) s = fma(sh.gamma[r], Z[(long long)r * P + c], s);
+    sh.gtz[c] = s / dtg;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x + 1; c < P; c += blockDim.x) {
+    double gc = sh.gtz[c], s = 0.0;
+    for (int r = 0; r < P; r++) {
+      double z = Z[(long long)r * P + c] - gc * sh.delta[r];
+      Z[(long long)r * P + c] = z;
+      s = fma(z, z, s);
+    }
+    if (s < norm_Z && s > kNumPrecision) {
+      double sc = sqrt(norm_Z / s);
+      for (int r = 0; r < P; r++) Z[(long long)r * P + c] *= sc;
+    }
+  }
+  __syncthreads();
+  return norm_Z;
+}
+
+// BFGS_Powell::Optimize from sh.x (updated in place).  Returns the final cost.
+__device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls) {
+  const int P = a.P;
+  double* Z = sh.Z;
+  for (int i = threadIdx.x; i < P * P; i += blockDim.x) Z[i] = (i % (P + 1)) == 0 ? 1.0 : 0.0;
+  double norm_Z = -1.0;
+  double f = dec_eval(a, sh, sh.x, sh.g, b);
+  calls++;
+  if (a.early_stop && f < a.tol) return f;
+  double fprev = fabs(f + f + 1.0);
+  for (;;) {
+    for (int c = threadIdx.x; c < P; c += blockDim.x) {
+      double s = 0.0;
+      for (int r = 0; r < P; r++) s = fma(Z[(long long)r * P + c], sh.g[r], s);
+      sh.ztg[c] = s;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < P; r += blockDim.x) {
+      const double* row = Z + (long long)r * P;
+      double s = 0.0;
+      for (int c = 0; c < P; c++) s = fma(-row[c], sh.ztg[c], s);
+      sh.d[r] = s;
+    }
+    __syncthreads();
+    double dg = dot(sh.d, sh.g, P, sh.scratch);
+    double max_step = 0.0;
+    if (dg < 0.0) {
+      double ms = INFINITY;
+      for (int k = threadIdx.x; k < P; k += blockDim.x)
+        if (fabs(sh.d[k]) >= 1e-5) ms = fmin(ms, fabs(kTwoPi / sh.d[k]));
+      ms = block_allmin(ms, sh.scratch);
+      max_step = isinf(ms) ? 0.0 : ms;
+    }
+    double gn = dot(sh.g, sh.g, P, sh.scratch);
+    if (gn <= 1e-19 * 1e-19 || dg >= 0.0 || f >= fprev) break;
+    fprev = f;
+    if (calls >= a.max_calls) break;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      sh.x0[i] = sh.x[i];
+      sh.g0[i] = sh.g[i];
+      sh.gbest[i] = sh.g[i];
+    }
+    __syncthreads();
+    double step = fmin(1.0, max_step);
+    double f_low = f, f_high = f, s_high = max_step, s_low = 0.0, s_best = 0.0, f_best = f, dg_best = fabs(dg);
+    double dg_high = 0.0;
+    for (int it = 0; it < 50; it++) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.x0[i] + step * sh.d[i];
+      __syncthreads();
+      f = dec_eval(a, sh, sh.x, sh.g, b);
+      calls++;
+      if (a.early_stop && f < a.tol) return f;
+      double dgc = dot(sh.d, sh.g, P, sh.scratch);
+      if (f < f_best || fabs(dgc) < dg_best) {
+        s_best = step;
+        f_best = f;
+        dg_best = fabs(dgc);
+        for (int i = threadIdx.x; i < P; i += blockDim.x) sh.gbest[i] = sh.g[i];
+        __syncthreads();
+      }
+      if (calls == a.max_calls) break;
+      if (f < f_low + step * 0.1 * dg) {
+        if (dgc >= dg * 0.7) break;
+        s_low = step;
+        f_low = f;
+      } else {
+        s_high = step;
+        f_high = f;
+        dg_high = dgc;
+      }
+      if (it == 0 || s_low > 0.0) {
+        double dlf = (f_high - f_low) / (s_high - s_low) * 2.0 - dg_high;
+        double scale = -dlf * 0.5 / (dg_high - dlf);
+        scale = fmax(0.1, scale);
+        step = s_low + scale * (s_high - s_low);
+      } else {
+        step = step * 0.1;
+        if (step < kNumPrecision) break;
+      }
+    }
+    if (step != s_best) {
+      step = s_best;
+      f = f_best;
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        sh.g[i] = sh.gbest[i];
+        sh.x[i] = sh.x0[i] + step * sh.d[i];
+      }
+      __syncthreads();
+    }
+    if (step == 0.0) break;
+    norm_Z = dec_bfgs_update(a, sh, norm_Z);
+  }
+  return f;
+}
+
+__global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
+  extern __shared__ double2 smem2[];
+  const int b = blockIdx.x;
+  if (b >= a.B) return;
+  const int P = a.P, L = a.L, NC = a.N * a.cols;
+  Sh sh;
+  char* p = reinterpret_cast<char*>(smem2);
+  auto take = [&](size_t bytes) { char* r = p; p += (bytes + 15) / 16 * 16; return r; };
+  sh.psi = (double2*)take(sizeof(double2) * NC);
+  sh.lam = (double2*)take(sizeof(double2) * NC);
+  sh.gm = (GateMat*)take(sizeof(GateMat) * max(L, 1));
+  sh.sc = (double2*)take(sizeof(double2) * max(P, 1));
+  sh.T = (double2*)take(sizeof(double2) * max(P, 1));
+  double** vecs[] = {&sh.x, &sh.g, &sh.d, &sh.x0, &sh.g0, &sh.gbest, &sh.ztg, &sh.delta, &sh.gamma,
+                     &sh.gtz, &sh.nz, &sh.bestx, &sh.guess, &sh.S};
+  for (double** v : vecs) *v = (double*)take(sizeof(double) * max(P, 1));
+  sh.redd = (double*)take(sizeof(double) * kTileMaxWarps * 8);
+  sh.tot = (double*)take(sizeof(double) * 8);
+  sh.scratch = (double*)take(sizeof(double) * kTileMaxWarps);
+  sh.Z = a.z_in_smem ? (double*)take(sizeof(double) * P * P) : a.zglob + (long long)b * P * P;
+
+  for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = a.x[(long long)b * P + i];
+  __syncthreads();
+  double best = INFINITY;
+  int calls = 0;
+  unsigned long long ctr = a.seed * 0x2545F4914F6CDD1DULL + (unsigned long long)b * 0x9E3779B97F4A7C15ULL;
+  bool done = false;
+  for (int outer = 0; outer < a.max_outer && !done; outer++) {
+    for (int loop = 0; loop < a.loops; loop++) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.guess[i];
+      __syncthreads();
+      double f = dec_bfgs(a, sh, b, calls);
+      for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = sh.x[i];
+      __syncthreads();
+      if (f < best) {
+        best = f;
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+          sh.bestx[i] = sh.x[i];
+          sh.guess[i] = sh.x[i] + u01(ctr + i) * kTwoPi / 100.0;
+        }
+        ctr += 0x100000001ULL * (unsigned long long)(P + 1);
+        __syncthreads();
+      }
+      if (a.early_stop && best < a.tol) {
+        done = true;
+        break;
+      }
+    }
+    for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = sh.bestx[i];
+    __syncthreads();
+    if (fabs(best) < a.tol) done = true;
+  }
+  for (int i = threadIdx.x; i < P; i += blockDim.x) a.x[(long long)b * P + i] = sh.bestx[i];
+  if (threadIdx.x == 0) {
+    a.cost[b] = best;
+    a.calls[b] = calls;
+  }
+}
+
+size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem) {
+  auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
+  size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
+  size_t s = 2 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + 2 * r16(sizeof(double2) * P) +
+             14 * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
+             r16(sizeof(double) * kTileMaxWarps);
+  if (z_in_smem) s += r16(sizeof(double) * P * P);
+  return s;
+}
+
+constexpr size_t kDecSmemLimit = 110 * 1024;  // keep two CTAs per SM
+
+}  // namespace
+
+extern "C" {
+
+size_t sqg_decompose_workspace_bytes(const sqg_circuit* c, int batch, int cols) {
+  if (!c || batch <= 0 || cols <= 0) return 0;
+  if (dec_smem_bytes(c, cols, true) <= kDecSmemLimit) return 256;
+  return (size_t)batch * c->P * c->P * sizeof(double) + 256;
+}
+
+int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, int batch, int trace_offset,
+                          int cost_variant, double* x, double* cost, int* calls, double tolerance, int max_calls,
+                          int max_outer, int iteration_loops, int stop_at_tolerance, unsigned long long seed,
+                          void* workspace, size_t ws_bytes, void* stream) {
+  if (!c || !targets || !x || !cost || !calls || batch <= 0 || batch > 0x7fffffff / 2 || cols <= 0 || cols > c->N)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "bad circuit, batch, targets or outputs");
+  if (c->P == 0) return set_error(SQG_ERR_INVALID_ARGUMENT, "the circuit has no free parameters");
+  if (cost_variant != SQG_FROBENIUS_NORM && cost_variant != SQG_HILBERT_SCHMIDT_TEST && cost_variant != SQG_INFIDELITY)
+    return set_error(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
+  const int off = cost_variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
+  if (off < 0 || off + cols > c->N) return set_error(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
+  if (c->n > 5) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 5");
+  if (max_calls < 1 || max_outer < 1 || iteration_loops < 1)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
+  bool zs = dec_smem_bytes(c, cols, true) <= kDecSmemLimit;
+  size_t smem = dec_smem_bytes(c, cols, zs);
+  if (smem > 227 * 1024) return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
+  if (!zs && (!workspace || ws_bytes < (size_t)batch * c->P * c->P * sizeof(double)))
+    return set_error(SQG_ERR_WORKSPACE, "workspace too small for the per-instance BFGS matrices");
+  DecArgs a;
+  a.gates = c->d_gates;
+  a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N; a.cols = cols;
+  a.trace_offset = off;
+  a.variant = cost_variant;
+  a.targets = (const double2*)targets;
+  a.tstride = (long long)c->N * cols;
+  a.x = x; a.cost = cost; a.calls = calls;
+  a.B = batch;
+  a.tol = tolerance;
+  a.max_calls = max_calls; a.max_outer = max_outer; a.loops = iteration_loops;
+  a.early_stop = stop_at_tolerance;
+  a.seed = seed;
+  a.zglob = (double*)workspace;
+  a.z_in_smem = zs ? 1 : 0;
+  cudaError_t e = cudaFuncSetAttribute(k_decompose, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  k_decompose<<<batch, kDecThreads, smem, (cudaStream_t)stream>>>(a);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
+}
+
+}  // extern "C"

@@ -27,24 +27,23 @@
 
 #include "../../include/sqg.h"
 #include "gates.cuh"
+#include "handle.h"
+#include "tile.cuh"
 
 using namespace sqg;
 
-struct sqg_circuit {
-  int n = 0, N = 0, L = 0, P = 0;
-  int device = 0;
-  Gate* d_gates = nullptr;
-  std::vector<Gate> h_gates;
-};
-
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
 
-int fail(int status, const std::string& msg) {
+int sqg::set_error(int status, const std::string& msg) {
   g_last_error = msg;
   return status;
 }
+
+namespace {
+
+int fail(int status, const std::string& msg) { return sqg::set_error(status, msg); }
 
 int cuda_status(cudaError_t e, const char* where) {
   if (e == cudaSuccess) return SQG_OK;
@@ -122,25 +121,6 @@ struct TileArgs {
   int nck;
 };
 
-// Applies one gate to every vector of the tile.  s holds tc vectors of length N.
-__device__ __forceinline__ void tile_apply(double2* s, int N, int logN, int tc, const Gate& gt, const PairOp& op) {
-  const bool ctrl = gate_controlled(gt.type);
-  const int lognp = ctrl ? logN - 2 : logN - 1;
-  const int npairs = 1 << lognp;
-  const int items = tc << lognp;
-  const int step = 1 << gt.target;
-  for (int it = threadIdx.x; it < items; it += blockDim.x) {
-    int col = it >> lognp;
-    int p = it & (npairs - 1);
-    int i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
-    double2* v = s + col * N;
-    double2 x = v[i], y = v[i + step];
-    apply_op(op, x, y);
-    v[i] = x;
-    v[i + step] = y;
-  }
-}
-
 __device__ __forceinline__ void load_tile(double2* s, const TileArgs& a, int b, int v0, int tc) {
   const double2* base = a.mtx + (long long)b * a.bstride;
   const int total = a.N * tc;
@@ -175,23 +155,6 @@ __device__ __forceinline__ void store_tile(const double2* s, const TileArgs& a, 
   }
 }
 
-// Block-wide sum of a complex value; result valid in thread 0.
-__device__ __forceinline__ double2 block_sum2(double2 v, double2* red) {
-  for (int o = 16; o > 0; o >>= 1) {
-    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-  }
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
-  if (nw == 1) return v;
-  if (lane == 0) red[w] = v;
-  __syncthreads();
-  double2 t = make_double2(0.0, 0.0);
-  if (threadIdx.x == 0)
-    for (int k = 0; k < nw; k++) { t.x += red[k].x; t.y += red[k].y; }
-  __syncthreads();
-  return t;
-}
-
 // Forward (or right) application of the whole circuit to one tile; optionally writes
 // the tile back and/or the traced diagonal partial.
 template <bool WRITE_BACK, bool TRACE>
@@ -214,51 +177,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_tile_forward(TileArgs a) {
     __syncthreads();
   }
   if (TRACE) {
-    double2 t = make_double2(0.0, 0.0);
-    for (int c = threadIdx.x; c < tc; c += blockDim.x) {
-      int row = v0 + c + a.trace_offset;
-      double2 v = s[c * a.N + row];
-      t.x += v.x;
-      t.y += v.y;
-    }
-    t = block_sum2(t, red);
+    double2 t = tile_trace(s, a.N, tc, v0, a.trace_offset, reinterpret_cast<double*>(red));
     if (threadIdx.x == 0) a.ws_tr[(long long)b * a.tiles + tile] = t;
   }
   if (WRITE_BACK) store_tile(s, a, b, v0, tc);
-}
-
-// Warp reduce-scatter of 8 doubles: afterwards lane l holds the warp total of value
-// (l >> 2) & 7 (9 FP64 adds per lane instead of 40 for eight full butterflies).
-__device__ __forceinline__ double warp_reduce_scatter8(double r[8]) {
-  const int lane = threadIdx.x & 31;
-  {
-    const bool hi = lane & 16;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      double send = hi ? r[k] : r[k + 4];
-      double keep = hi ? r[k + 4] : r[k];
-      r[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-  }
-  {
-    const bool hi = lane & 8;
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      double send = hi ? r[k] : r[k + 2];
-      double keep = hi ? r[k + 2] : r[k];
-      r[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-  }
-  {
-    const bool hi = lane & 4;
-    double send = hi ? r[0] : r[1];
-    double keep = hi ? r[1] : r[0];
-    r[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-  }
-  double v = r[0];
-  v += __shfl_xor_sync(0xffffffffu, v, 2);
-  v += __shfl_xor_sync(0xffffffffu, v, 1);
-  return v;
 }
 
 // Cost + adjoint gradient of one (instance, tile).
@@ -269,12 +191,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_tile_adjoint(TileArgs a) {
   double2* lam = smem + (size_t)a.TC * N;
   double* redd = reinterpret_cast<double*>(lam + (size_t)a.TC * N);  // [kMaxWarps][8]
   double* tot = redd + kMaxWarps * 8;                                 // [8]
-  double2* red2 = reinterpret_cast<double2*>(tot + 8);                // [kMaxWarps]
+  double* scratch = tot + 8;                                          // [kMaxWarps]
   const int b = blockIdx.y, tile = blockIdx.x;
   const int v0 = tile * a.TC;
   const int tc = min(a.TC, a.cols - v0);
-  const int nw = (blockDim.x + 31) >> 5;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t tile_elems = (size_t)a.TC * N;
   double2* ck = a.ckpt ? a.ckpt + ((long long)b * a.tiles + tile) * a.nck * tile_elems : nullptr;
 
@@ -287,7 +207,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_tile_adjoint(TileArgs a) {
   __syncthreads();
   const GateMat* gm = a.gm + (long long)b * a.L;
   const double2* scb = a.sc + (long long)b * a.P;
-  // forward sweep
+  // forward sweep, storing psi after every ckpt_interval-th gate
   for (int g = 0; g < a.L; g++) {
     Gate gt = a.gates[g];
     PairOp op = make_op(gt.type, gm[g], ORIENT_FWD);
@@ -298,95 +218,22 @@ __global__ void __launch_bounds__(kMaxThreads) k_tile_adjoint(TileArgs a) {
       for (int e = threadIdx.x; e < tc * N; e += blockDim.x) dst[e] = psi[e];
     }
   }
-  // forward trace partial
-  {
-    double2 t = make_double2(0.0, 0.0);
-    for (int c = threadIdx.x; c < tc; c += blockDim.x) {
-      double2 v = psi[c * N + v0 + c + a.trace_offset];
-      t.x += v.x;
-      t.y += v.y;
-    }
-    t = block_sum2(t, red2);
-    if (threadIdx.x == 0) a.ws_tr[(long long)b * a.tiles + tile] = t;
-  }
+  double2 t = tile_trace(psi, N, tc, v0, a.trace_offset, scratch);
+  if (threadIdx.x == 0) a.ws_tr[(long long)b * a.tiles + tile] = t;
   double2* wgr = a.ws_gr + ((long long)b * a.tiles + tile) * a.P;
-  // reverse sweep
-  for (int g = a.L - 1; g >= 0; g--) {
-    Gate gt = a.gates[g];
+  auto sink = [&](int p, double2 v) { wgr[p] = v; };
+  // before reverse step g, psi must hold the state after gate g; restore the stored copy
+  // at checkpoint boundaries so that uncomputation error never spans more than
+  // ckpt_interval gates
+  auto restore = [&](int g) {
     if (ck && (g + 1) % a.ckpt_interval == 0 && (g + 1) / a.ckpt_interval <= a.nck && g + 1 < a.L) {
-      // psi currently holds the uncomputed state after gate g; restore the stored one
       const double2* src = ck + (size_t)((g + 1) / a.ckpt_interval - 1) * tile_elems;
       __syncthreads();
       for (int e = threadIdx.x; e < tc * N; e += blockDim.x) psi[e] = src[e];
       __syncthreads();
     }
-    PairOp op = make_op(gt.type, gm[g], ORIENT_ADJ);
-    const int np = gate_param_num(gt.type);
-    if (np == 0) {
-      tile_apply(psi, N, logN, tc, gt, op);
-      tile_apply(lam, N, logN, tc, gt, op);
-      __syncthreads();
-      continue;
-    }
-    const bool ctrl = gate_controlled(gt.type);
-    const int lognp = ctrl ? logN - 2 : logN - 1;
-    const int npairs = 1 << lognp;
-    const int items = tc << lognp;
-    const int step = 1 << gt.target;
-    double r[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) r[k] = 0.0;
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
-      int col = it >> lognp;
-      int p = it & (npairs - 1);
-      int i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
-      double2* ps = psi + col * N;
-      double2* ls = lam + col * N;
-      double2 x = ps[i], y = ps[i + step];
-      apply_op(op, x, y);  // psi before gate g
-      ps[i] = x;
-      ps[i + step] = y;
-      double2 lx = ls[i], ly = ls[i + step];
-      // R_ab += conj(lambda_a) psi_b
-      r[0] = fma(lx.x, x.x, fma(lx.y, x.y, r[0]));
-      r[1] = fma(lx.x, x.y, fma(-lx.y, x.x, r[1]));
-      r[2] = fma(lx.x, y.x, fma(lx.y, y.y, r[2]));
-      r[3] = fma(lx.x, y.y, fma(-lx.y, y.x, r[3]));
-      r[4] = fma(ly.x, x.x, fma(ly.y, x.y, r[4]));
-      r[5] = fma(ly.x, x.y, fma(-ly.y, x.x, r[5]));
-      r[6] = fma(ly.x, y.x, fma(ly.y, y.y, r[6]));
-      r[7] = fma(ly.x, y.y, fma(-ly.y, y.x, r[7]));
-      apply_op(op, lx, ly);  // lambda before gate g
-      ls[i] = lx;
-      ls[i + step] = ly;
-    }
-    double v = warp_reduce_scatter8(r);
-    if (nw == 1) {
-      if ((lane & 3) == 0) tot[lane >> 2] = v;
-    } else if ((lane & 3) == 0) {
-      redd[warp * 8 + (lane >> 2)] = v;
-    }
-    __syncthreads();
-    if (nw > 1 && threadIdx.x < 8) {
-      double t = 0.0;
-      for (int w = 0; w < nw; w++) t += redd[w * 8 + threadIdx.x];
-      tot[threadIdx.x] = t;
-    }
-    if (nw > 1) __syncthreads();
-    if (threadIdx.x < np) {
-      double2 D[4];
-      deriv_kernel(gt.type, scb + gt.pstart, threadIdx.x, D);
-      // T = sum_ab D_ab R_ab
-      double tr = 0.0, ti = 0.0;
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        double rr = tot[2 * k], ri = tot[2 * k + 1];
-        tr = fma(D[k].x, rr, fma(-D[k].y, ri, tr));
-        ti = fma(D[k].x, ri, fma(D[k].y, rr, ti));
-      }
-      wgr[gt.pstart + threadIdx.x] = make_double2(tr, ti);
-    }
-  }
+  };
+  adjoint_sweep(psi, lam, N, logN, tc, a.gates, gm, scb, a.L, redd, tot, sink, restore);
 }
 
 // Sums the per-tile partials in a fixed order and applies the cost-variant epilogue of
@@ -525,8 +372,7 @@ TilePlan plan_tiles(int N, int cols, bool grad) {
   pl.TC = tc;
   pl.tiles = (cols + tc - 1) / tc;
   pl.threads = choose_threads(tc, N, grad);
-  size_t extra = grad ? (kMaxWarps * 8 + 8) * sizeof(double) + kMaxWarps * sizeof(double2)
-                      : kMaxWarps * sizeof(double2);
+  size_t extra = grad ? (kMaxWarps * 8 + 8 + kMaxWarps) * sizeof(double) : kMaxWarps * sizeof(double2);
   pl.smem = per * tc + extra;
   return pl;
 }

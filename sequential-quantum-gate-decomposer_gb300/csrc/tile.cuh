@@ -1,0 +1,221 @@
+// Shared-memory column-tile sweeps used by the evaluator kernels (engine.cu) and the
+// batched decomposition kernel (decompose.cu).
+//
+// A tile holds tc vectors of length N (one column of the target each, column-major in
+// shared memory).  Every routine is executed by all threads of the CTA; blockDim.x is a
+// multiple of 32 and at most kTileMaxThreads.
+#pragma once
+#include "gates.cuh"
+
+namespace sqg {
+
+constexpr int kTileMaxThreads = 256;
+constexpr int kTileMaxWarps = kTileMaxThreads / 32;
+
+// Applies one gate to every vector of the tile.
+__device__ __forceinline__ void tile_apply(double2* s, int N, int logN, int tc, const Gate& gt, const PairOp& op) {
+  const bool ctrl = gate_controlled(gt.type);
+  const int lognp = ctrl ? logN - 2 : logN - 1;
+  const int npairs = 1 << lognp;
+  const int items = tc << lognp;
+  const int step = 1 << gt.target;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    int col = it >> lognp;
+    int p = it & (npairs - 1);
+    int i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
+    double2* v = s + col * N;
+    double2 x = v[i], y = v[i + step];
+    apply_op(op, x, y);
+    v[i] = x;
+    v[i + step] = y;
+  }
+}
+
+// Warp reduce-scatter of 8 doubles: afterwards lane l holds the warp total of value
+// (l >> 2) & 7 (9 FP64 adds per lane instead of 40 for eight full butterflies).
+__device__ __forceinline__ double warp_reduce_scatter8(double r[8]) {
+  const int lane = threadIdx.x & 31;
+  {
+    const bool hi = lane & 16;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      double send = hi ? r[k] : r[k + 4];
+      double keep = hi ? r[k + 4] : r[k];
+      r[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+  }
+  {
+    const bool hi = lane & 8;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      double send = hi ? r[k] : r[k + 2];
+      double keep = hi ? r[k + 2] : r[k];
+      r[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+  }
+  {
+    const bool hi = lane & 4;
+    double send = hi ? r[0] : r[1];
+    double keep = hi ? r[1] : r[0];
+    r[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  double v = r[0];
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v;
+}
+
+// Sum of v over the CTA, returned to every thread (fixed summation order, so all threads
+// hold the identical value).  scratch: kTileMaxWarps doubles.
+__device__ __forceinline__ double block_allsum(double v, double* scratch) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int nw = blockDim.x >> 5;
+  if (nw == 1) return v;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < nw; w++) t += scratch[w];
+  return t;
+}
+
+__device__ __forceinline__ double block_allmin(double v, double* scratch) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int nw = blockDim.x >> 5;
+  if (nw == 1) return v;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = scratch[0];
+  for (int w = 1; w < nw; w++) t = fmin(t, scratch[w]);
+  return t;
+}
+
+// Complex trace partial sum_c s[c][v0 + c + offset] over the tile, returned to all threads.
+__device__ __forceinline__ double2 tile_trace(const double2* s, int N, int tc, int v0, int offset, double* scratch) {
+  double2 t = make_double2(0.0, 0.0);
+  for (int c = threadIdx.x; c < tc; c += blockDim.x) {
+    double2 v = s[c * N + v0 + c + offset];
+    t.x += v.x;
+    t.y += v.y;
+  }
+  t.x = block_allsum(t.x, scratch);
+  t.y = block_allsum(t.y, scratch);
+  return t;
+}
+
+// Reverse (adjoint) sweep over gates L-1..0.  On entry psi holds C u_j and lam holds
+// e_{j + offset} for each vector of the tile.  For every parametric gate the
+// contraction T_k = sum_ab D_ab R_ab with R_ab = sum conj(lambda_a) psi_b (psi before
+// the gate, lambda after it) is handed to sink(param_index, T) by threads 0..np-1.
+// redd: kTileMaxWarps * 8 doubles, tot: 8 doubles.  restore(g) is called at the start of
+// each reverse step and may overwrite psi (checkpoints); it must contain its own barriers.
+template <class Sink, class Restore>
+__device__ __forceinline__ void adjoint_sweep(double2* psi, double2* lam, int N, int logN, int tc, const Gate* gates,
+                                              const GateMat* gm, const double2* sc, int L, double* redd, double* tot,
+                                              Sink sink, Restore restore) {
+  const int nw = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int g = L - 1; g >= 0; g--) {
+    restore(g);
+    Gate gt = gates[g];
+    PairOp op = make_op(gt.type, gm[g], ORIENT_ADJ);
+    const int np = gate_param_num(gt.type);
+    if (np == 0) {
+      tile_apply(psi, N, logN, tc, gt, op);
+      tile_apply(lam, N, logN, tc, gt, op);
+      __syncthreads();
+      continue;
+    }
+    const bool ctrl = gate_controlled(gt.type);
+    const int lognp = ctrl ? logN - 2 : logN - 1;
+    const int npairs = 1 << lognp;
+    const int items = tc << lognp;
+    const int step = 1 << gt.target;
+    double r[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) r[k] = 0.0;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      int col = it >> lognp;
+      int p = it & (npairs - 1);
+      int i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
+      double2* ps = psi + col * N;
+      double2* ls = lam + col * N;
+      double2 x = ps[i], y = ps[i + step];
+      apply_op(op, x, y);  // psi in front of gate g
+      ps[i] = x;
+      ps[i + step] = y;
+      double2 lx = ls[i], ly = ls[i + step];
+      r[0] = fma(lx.x, x.x, fma(lx.y, x.y, r[0]));
+      r[1] = fma(lx.x, x.y, fma(-lx.y, x.x, r[1]));
+      r[2] = fma(lx.x, y.x, fma(lx.y, y.y, r[2]));
+      r[3] = fma(lx.x, y.y, fma(-lx.y, y.x, r[3]));
+      r[4] = fma(ly.x, x.x, fma(ly.y, x.y, r[4]));
+      r[5] = fma(ly.x, x.y, fma(-ly.y, x.x, r[5]));
+      r[6] = fma(ly.x, y.x, fma(ly.y, y.y, r[6]));
+      r[7] = fma(ly.x, y.y, fma(-ly.y, y.x, r[7]));
+      apply_op(op, lx, ly);  // lambda in front of gate g
+      ls[i] = lx;
+      ls[i + step] = ly;
+    }
+    double v = warp_reduce_scatter8(r);
+    if (nw == 1) {
+      if ((lane & 3) == 0) tot[lane >> 2] = v;
+    } else if ((lane & 3) == 0) {
+      redd[warp * 8 + (lane >> 2)] = v;
+    }
+    __syncthreads();
+    if (nw > 1) {
+      if (threadIdx.x < 8) {
+        double t = 0.0;
+        for (int w = 0; w < nw; w++) t += redd[w * 8 + threadIdx.x];
+        tot[threadIdx.x] = t;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x < np) {
+      double2 D[4];
+      deriv_kernel(gt.type, sc + gt.pstart, threadIdx.x, D);
+      double tr = 0.0, ti = 0.0;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        double rr = tot[2 * k], ri = tot[2 * k + 1];
+        tr = fma(D[k].x, rr, fma(-D[k].y, ri, tr));
+        ti = fma(D[k].x, ri, fma(D[k].y, rr, ti));
+      }
+      sink(gt.pstart + threadIdx.x, make_double2(tr, ti));
+    }
+  }
+}
+
+// Builds the gate matrices and per-parameter (sin, cos) of one parameter vector
+// (threads over gates).  Same formulas as k_prep in engine.cu.
+__device__ __forceinline__ void build_gate_mats(const Gate* gates, int L, const double* th, GateMat* gm, double2* sc) {
+  for (int g = threadIdx.x; g < L; g += blockDim.x) {
+    Gate gt = gates[g];
+    GateMat m;
+    m.u[0] = m.u[1] = m.u[2] = m.u[3] = make_double2(0.0, 0.0);
+    if (gt.type == G_U3) {
+      double st, ct, sp, cp, sl, cl;
+      sincos(th[gt.pstart], &st, &ct);
+      sincos(th[gt.pstart + 1], &sp, &cp);
+      sincos(th[gt.pstart + 2], &sl, &cl);
+      sc[gt.pstart] = make_double2(st, ct);
+      sc[gt.pstart + 1] = make_double2(sp, cp);
+      sc[gt.pstart + 2] = make_double2(sl, cl);
+      double spl = sp * cl + cp * sl, cpl = cp * cl - sp * sl;
+      m.u[0] = make_double2(ct, 0.0);
+      m.u[1] = make_double2(-st * cl, -st * sl);
+      m.u[2] = make_double2(st * cp, st * sp);
+      m.u[3] = make_double2(ct * cpl, ct * spl);
+    } else if (gate_param_num(gt.type) == 1) {
+      double s, c;
+      sincos(th[gt.pstart], &s, &c);
+      sc[gt.pstart] = make_double2(s, c);
+      m.u[0] = make_double2(c, s);
+    }
+    gm[g] = m;
+  }
+}
+
+}  // namespace sqg

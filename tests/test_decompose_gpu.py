@@ -1,0 +1,79 @@
+"""Batched on-device decomposition (sqg_decompose_batched) against the oracle's BFGS
+driver and the cost it certifies."""
+import importlib
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def wl():
+    return importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+
+
+def test_first_bfgs_steps_follow_the_oracle(sqg, wl):
+    """With a small evaluation budget and no tolerance stop, the device BFGS lands where
+    the oracle's restatement of BFGS_Powell lands."""
+    n = 3
+    rng = np.random.default_rng(41)
+    c = wl.cnot_u3_ansatz(n, 5)
+    P = c.get_Parameter_Num()
+    recs = c.gate_records()
+    B = 6
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, recs, rng.uniform(0, 2 * np.pi, P)).conj().T)
+                        for _ in range(B)])
+    x0 = rng.uniform(0, 2 * np.pi, (B, P))
+    dec = sqg.BatchedDecomposer(c, tolerance=0.0, max_calls=6, max_outer=1, stop_at_tolerance=False)
+    x, cost, calls = dec.run(targets, x0)
+    torch.cuda.synchronize()
+    xr, cr, callr = O.decompose(n, recs, targets, x0, tolerance=0.0, max_inner=6, max_outer=1)
+    assert np.array_equal(calls.cpu().numpy(), callr)
+    assert np.allclose(cost.cpu().numpy(), cr, rtol=1e-9, atol=1e-12)
+    assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)
+
+
+@pytest.mark.parametrize("n,blocks", [(2, 3), (3, 8)])
+def test_batched_decomposition_reaches_tolerance(sqg, wl, n, blocks):
+    rng = np.random.default_rng(50 + n)
+    c = wl.cnot_u3_ansatz(n, blocks)
+    P = c.get_Parameter_Num()
+    recs = c.gate_records()
+    B = 24
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, recs, rng.uniform(0, 2 * np.pi, P)).conj().T)
+                        for _ in range(B)])
+    x0 = rng.uniform(0, 2 * np.pi, (B, P))
+    dec = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=3000, max_outer=4)
+    x, cost, calls = dec.run(targets, x0, seed=7)
+    x2, cost2, calls2 = dec.run(targets, x0, seed=7)
+    torch.cuda.synchronize()
+    xs, cs = x.cpu().numpy(), cost.cpu().numpy()
+    assert np.array_equal(xs, x2.cpu().numpy()) and np.array_equal(cs, cost2.cpu().numpy())
+    ok = cs < 1e-8
+    assert ok.mean() >= 0.75, cs
+    for b in np.nonzero(ok)[0]:
+        assert O.cost(n, recs, xs[b], targets[b]) < 1e-8
+    assert np.all(calls.cpu().numpy() <= 4 * 3000)
+
+
+def test_exact_start_stops_after_one_evaluation(sqg, wl):
+    n = 3
+    rng = np.random.default_rng(60)
+    c = wl.cnot_u3_ansatz(n, 4)
+    P = c.get_Parameter_Num()
+    p = rng.uniform(0, 2 * np.pi, (3, P))
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, c.gate_records(), p[b]).conj().T) for b in range(3)])
+    x, cost, calls = sqg.BatchedDecomposer(c).run(targets, p)
+    torch.cuda.synchronize()
+    assert np.all(calls.cpu().numpy() == 1)
+    assert np.all(cost.cpu().numpy() < 1e-12)
+
+
+def test_rejects_unsupported(sqg, wl):
+    c = wl.cnot_u3_ansatz(6, 2)
+    with pytest.raises(Exception):
+        sqg.BatchedDecomposer(c).run(np.zeros((1, 64, 64), dtype=np.complex128), np.zeros((1, c.get_Parameter_Num())))
