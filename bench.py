@@ -33,7 +33,7 @@ UNIT = "decompositions/s"
 N_TARGETS = 4096
 ANSATZ_BLOCKS = 14
 TOL = 1e-8
-MAX_CALLS = 2000      # cost+gradient evaluations per BFGS run
+MAX_CALLS = 1000      # cost+gradient evaluations per BFGS run
 MAX_OUTER = 4         # restarts (N_Qubit_Decomposition_custom uses 4 outer iterations)
 
 
@@ -368,8 +368,38 @@ def bench_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def profile_case(case):
+    """Small single-launch cases for ncu captures (one kernel of interest each)."""
+    import torch
+
+    sqg = importlib.import_module(PKG)
+    wl = importlib.import_module(PKG + ".workloads")
+    rng = np.random.default_rng(3)
+    if case == "decompose":
+        ansatz, targets = make_workload(sqg, wl)
+        P = ansatz.get_Parameter_Num()
+        B = 1216
+        dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=60, max_outer=1)
+        x, cost, calls = dec.run(torch.from_numpy(targets[:B]).cuda(), rng.uniform(0, 2 * np.pi, (B, P)))
+    elif case == "gate_apply":
+        c = wl.random_gate_circuit(12, 200, rng)
+        th = torch.from_numpy(rng.uniform(0, 2 * np.pi, (1, c.get_Parameter_Num()))).cuda()
+        m = torch.zeros((1, 4096, 4096), dtype=torch.complex128, device="cuda")
+        c.apply_to_device(th, m, fused=True)
+        c.apply_to_device(th, m, fused=False)
+    elif case == "cost_grad":
+        c = wl.cnot_u3_ansatz(8, 60)
+        P = c.get_Parameter_Num()
+        U = c.get_Matrix(rng.uniform(0, 2 * np.pi, P))
+        ev = sqg.CostEvaluator(c, np.ascontiguousarray(U.conj().T))
+        ev.cost_grad(torch.from_numpy(rng.uniform(0, 2 * np.pi, (64, P))).cuda())
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": case, "ok": True}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad"], default=None)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -379,6 +409,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--ref-targets", type=int, default=32)
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <string>
 
 #include "../../include/sqg.h"
@@ -46,8 +47,10 @@ struct DecArgs {
 };
 
 struct Sh {
-  double2 *psi, *lam, *sc, *T;
+  double2 *psi, *lam, *sc;
   GateMat* gm;
+  double* R;   // [L][8] reduced 2x2 overlaps of the reverse sweep
+  int* pgate;  // gate owning each parameter
   double *x, *g, *d, *x0, *g0, *gbest, *ztg, *delta, *gamma, *gtz, *nz, *bestx, *guess, *S;
   double *Z, *redd, *tot, *scratch;
 };
@@ -83,9 +86,14 @@ __device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, dou
     __syncthreads();
   }
   double2 tr = tile_trace(sh.psi, N, cols, 0, off, sh.scratch);
-  double2* Tp = sh.T;
+  double* Rb = sh.R;
+  // buffer each gate's overlap; the derivative contractions run afterwards for all
+  // parameters at once on full warps
   adjoint_sweep(sh.psi, sh.lam, N, a.n, cols, a.gates, sh.gm, sh.sc, a.L, sh.redd, sh.tot,
-                [&](int p, double2 v) { Tp[p] = v; }, [](int) {});
+                [&](int g, const Gate&, const double* R) {
+                  if (threadIdx.x < 8) Rb[g * 8 + threadIdx.x] = R[threadIdx.x];
+                },
+                [](int) {});
   __syncthreads();
   double f;
   const double dc = cols;
@@ -98,7 +106,9 @@ __device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, dou
     f = 1.0 - ((tr.x * tr.x + tr.y * tr.y) / dc + 1) / (dc + 1);
   }
   for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
-    double2 t = Tp[p];
+    const int g = sh.pgate[p];
+    const Gate gt = a.gates[g];
+    double2 t = contract_derivative(gt, sh.sc, p - gt.pstart, Rb + g * 8);
     double gvv;
     if (a.variant == SQG_FROBENIUS_NORM) {
       gvv = (1.0 - t.x / dc) - 1.0;
@@ -303,7 +313,8 @@ __global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
   sh.lam = (double2*)take(sizeof(double2) * NC);
   sh.gm = (GateMat*)take(sizeof(GateMat) * max(L, 1));
   sh.sc = (double2*)take(sizeof(double2) * max(P, 1));
-  sh.T = (double2*)take(sizeof(double2) * max(P, 1));
+  sh.R = (double*)take(sizeof(double) * 8 * max(L, 1));
+  sh.pgate = (int*)take(sizeof(int) * max(P, 1));
   double** vecs[] = {&sh.x, &sh.g, &sh.d, &sh.x0, &sh.g0, &sh.gbest, &sh.ztg, &sh.delta, &sh.gamma,
                      &sh.gtz, &sh.nz, &sh.bestx, &sh.guess, &sh.S};
   for (double** v : vecs) *v = (double*)take(sizeof(double) * max(P, 1));
@@ -312,6 +323,10 @@ __global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
   sh.scratch = (double*)take(sizeof(double) * kTileMaxWarps);
   sh.Z = a.z_in_smem ? (double*)take(sizeof(double) * P * P) : a.zglob + (long long)b * P * P;
 
+  for (int g = threadIdx.x; g < L; g += blockDim.x) {
+    Gate gt = a.gates[g];
+    for (int k = 0; k < gate_param_num(gt.type); k++) sh.pgate[gt.pstart + k] = g;
+  }
   for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = a.x[(long long)b * P + i];
   __syncthreads();
   double best = INFINITY;
@@ -353,7 +368,8 @@ __global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
 size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem) {
   auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
-  size_t s = 2 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + 2 * r16(sizeof(double2) * P) +
+  size_t s = 2 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
+             r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) +
              14 * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
              r16(sizeof(double) * kTileMaxWarps);
   if (z_in_smem) s += r16(sizeof(double) * P * P);
@@ -362,13 +378,24 @@ size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem) {
 
 constexpr size_t kDecSmemLimit = 110 * 1024;  // keep two CTAs per SM
 
+// Per-instance BFGS matrices stay in shared memory only while they are small (<= 16 KB):
+// beyond that, keeping them in the caller's workspace (L2-resident for the ~1000
+// instances in flight) lets several times more instances share an SM, and the kernel
+// is bound by FP64 issue, not by L2.  SQG_DECOMPOSE_Z=global|shared overrides the rule.
+bool z_in_shared(const sqg_circuit* c, int cols) {
+  const char* zenv = getenv("SQG_DECOMPOSE_Z");
+  if (zenv && std::string(zenv) == "global") return false;
+  if (zenv && std::string(zenv) == "shared") return dec_smem_bytes(c, cols, true) <= 227 * 1024;
+  return (size_t)c->P * c->P * sizeof(double) <= 16 * 1024 && dec_smem_bytes(c, cols, true) <= kDecSmemLimit;
+}
+
 }  // namespace
 
 extern "C" {
 
 size_t sqg_decompose_workspace_bytes(const sqg_circuit* c, int batch, int cols) {
   if (!c || batch <= 0 || cols <= 0) return 0;
-  if (dec_smem_bytes(c, cols, true) <= kDecSmemLimit) return 256;
+  if (z_in_shared(c, cols)) return 256;
   return (size_t)batch * c->P * c->P * sizeof(double) + 256;
 }
 
@@ -386,7 +413,7 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   if (c->n > 5) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 5");
   if (max_calls < 1 || max_outer < 1 || iteration_loops < 1)
     return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
-  bool zs = dec_smem_bytes(c, cols, true) <= kDecSmemLimit;
+  const bool zs = z_in_shared(c, cols);
   size_t smem = dec_smem_bytes(c, cols, zs);
   if (smem > 227 * 1024) return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
   if (!zs && (!workspace || ws_bytes < (size_t)batch * c->P * c->P * sizeof(double)))
@@ -408,7 +435,9 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.z_in_smem = zs ? 1 : 0;
   cudaError_t e = cudaFuncSetAttribute(k_decompose, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-  k_decompose<<<batch, kDecThreads, smem, (cudaStream_t)stream>>>(a);
+  // one thread per parameter for the vector and Z-matrix work, at least two warps
+  const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
+  k_decompose<<<batch, threads, smem, (cudaStream_t)stream>>>(a);
   e = cudaGetLastError();
   return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
 }

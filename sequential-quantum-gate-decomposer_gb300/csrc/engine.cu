@@ -221,7 +221,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_tile_adjoint(TileArgs a) {
   double2 t = tile_trace(psi, N, tc, v0, a.trace_offset, scratch);
   if (threadIdx.x == 0) a.ws_tr[(long long)b * a.tiles + tile] = t;
   double2* wgr = a.ws_gr + ((long long)b * a.tiles + tile) * a.P;
-  auto sink = [&](int p, double2 v) { wgr[p] = v; };
+  auto sink = [&](int, const Gate& gt, const double* R) {
+    if (threadIdx.x < gate_param_num(gt.type)) wgr[gt.pstart + threadIdx.x] = contract_derivative(gt, scb, threadIdx.x, R);
+  };
   // before reverse step g, psi must hold the state after gate g; restore the stored copy
   // at checkpoint boundaries so that uncomputation error never spans more than
   // ckpt_interval gates

@@ -105,9 +105,12 @@ __device__ __forceinline__ double2 tile_trace(const double2* s, int N, int tc, i
 }
 
 // Reverse (adjoint) sweep over gates L-1..0.  On entry psi holds C u_j and lam holds
-// e_{j + offset} for each vector of the tile.  For every parametric gate the
-// contraction T_k = sum_ab D_ab R_ab with R_ab = sum conj(lambda_a) psi_b (psi before
-// the gate, lambda after it) is handed to sink(param_index, T) by threads 0..np-1.
+// e_{j + offset} for each vector of the tile.  For every parametric gate g the 2x2
+// overlap R_ab = sum conj(lambda_a) psi_b (psi in front of the gate, lambda behind it)
+// is reduced over the tile into tot[0..7] = (Re R00, Im R00, Re R01, Im R01, Re R10,
+// Im R10, Re R11, Im R11) and sink(g, gate, tot) is called by every thread.
+// Only the warps that own amplitude pairs of the gate take part in the reduction: the
+// FP64 pipe is charged per warp instruction whatever the number of active lanes.
 // redd: kTileMaxWarps * 8 doubles, tot: 8 doubles.  restore(g) is called at the start of
 // each reverse step and may overwrite psi (checkpoints); it must contain its own barriers.
 template <class Sink, class Restore>
@@ -158,34 +161,41 @@ __device__ __forceinline__ void adjoint_sweep(double2* psi, double2* lam, int N,
       ls[i] = lx;
       ls[i + step] = ly;
     }
-    double v = warp_reduce_scatter8(r);
-    if (nw == 1) {
-      if ((lane & 3) == 0) tot[lane >> 2] = v;
-    } else if ((lane & 3) == 0) {
-      redd[warp * 8 + (lane >> 2)] = v;
+    const int aw = min(nw, (items + 31) >> 5);  // warps holding pairs
+    if (warp < aw) {
+      double v = warp_reduce_scatter8(r);
+      if ((lane & 3) == 0) {
+        if (aw == 1)
+          tot[lane >> 2] = v;
+        else
+          redd[warp * 8 + (lane >> 2)] = v;
+      }
     }
     __syncthreads();
-    if (nw > 1) {
+    if (aw > 1) {
       if (threadIdx.x < 8) {
         double t = 0.0;
-        for (int w = 0; w < nw; w++) t += redd[w * 8 + threadIdx.x];
+        for (int w = 0; w < aw; w++) t += redd[w * 8 + threadIdx.x];
         tot[threadIdx.x] = t;
       }
       __syncthreads();
     }
-    if (threadIdx.x < np) {
-      double2 D[4];
-      deriv_kernel(gt.type, sc + gt.pstart, threadIdx.x, D);
-      double tr = 0.0, ti = 0.0;
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        double rr = tot[2 * k], ri = tot[2 * k + 1];
-        tr = fma(D[k].x, rr, fma(-D[k].y, ri, tr));
-        ti = fma(D[k].x, ri, fma(D[k].y, rr, ti));
-      }
-      sink(gt.pstart + threadIdx.x, make_double2(tr, ti));
-    }
+    sink(g, gt, tot);
   }
+}
+
+// T = sum_ab D_ab R_ab for derivative parameter k of gate gt, R as laid out in tot.
+__device__ __forceinline__ double2 contract_derivative(const Gate& gt, const double2* sc, int k, const double* R) {
+  double2 D[4];
+  deriv_kernel(gt.type, sc + gt.pstart, k, D);
+  double tr = 0.0, ti = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    double rr = R[2 * q], ri = R[2 * q + 1];
+    tr = fma(D[q].x, rr, fma(-D[q].y, ri, tr));
+    ti = fma(D[q].x, ri, fma(D[q].y, rr, ti));
+  }
+  return make_double2(tr, ti);
 }
 
 // Builds the gate matrices and per-parameter (sin, cos) of one parameter vector
