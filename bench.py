@@ -46,8 +46,9 @@ def peaks():
         return 6800.0, "fallback"
 
 
-# FP64 FMA pipe peak measured on this machine's GB300 with a dependent-free DFMA loop
-# (profiles/fp64_peak_probe.md): 1.20 TFLOP/s counting an FMA as 2 flops.
+# FP64 FMA pipe peak of the GB300 (TFLOP/s, an FMA counts 2 flops).  Measured live at the
+# start of every run by the engine's probe kernel (sqg_probe_fp64_tflops); 1.20 is the
+# value measured on the GB300s and is used only if the probe cannot run.
 FP64_PEAK_TFLOPS = 1.20
 
 
@@ -137,9 +138,12 @@ def fp64_ops_per_eval(circuit_records, N, cols):
 def bench_ours(args):
     import torch
 
+    global FP64_PEAK_TFLOPS
     sqg = importlib.import_module(PKG)
     wl = importlib.import_module(PKG + ".workloads")
+    native = importlib.import_module(PKG + "._native")
     torch.cuda.set_device(0)
+    FP64_PEAK_TFLOPS = max(native.probe_fp64_tflops() for _ in range(3))
     ansatz, targets = make_workload(sqg, wl)
     P = ansatz.get_Parameter_Num()
     dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=MAX_CALLS, max_outer=MAX_OUTER)
@@ -211,6 +215,7 @@ def bench_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "peak_source": "measured live by the FP64 probe kernel",
                      "frac": achieved_tflops / FP64_PEAK_TFLOPS, "traffic": None,
                      "note": "k_decompose is FP64-pipe bound (GB300 FP64 = 1.2 TFLOP/s measured); counts only the "
                              "cost+gradient FP64 ops, not the BFGS linear algebra"},
@@ -399,6 +404,7 @@ def profile_case(case):
 
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--probe-fp64", action="store_true", help="print the live FP64 FMA peak by active lanes")
     ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad"], default=None)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -409,6 +415,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--ref-targets", type=int, default=32)
     args = ap.parse_args()
+    if args.probe_fp64:
+        native = importlib.import_module(PKG + "._native")
+        print(json.dumps({"fp64_fma_tflops_by_active_lanes": {k: native.probe_fp64_tflops(k) for k in (32, 16, 8, 1)}}))
+        return
     if args.profile_case:
         profile_case(args.profile_case)
         return

@@ -12,8 +12,9 @@
  *   - parameters are contiguous in gate order; U3 stores (theta/2, phi, lambda),
  *     RX/RY/RZ/CRY store theta/2; kernels use sin/cos of the stored value.
  *
- * Every pointer argument named *_dev is device memory owned by the caller; the
- * engine allocates nothing.  Calls are asynchronous on the given CUDA stream
+ * Every pointer argument named *_dev is device memory owned by the caller; apart from
+ * the gate table that sqg_circuit_create copies to the device, the engine allocates no
+ * device memory.  Calls are asynchronous on the given CUDA stream
  * (cudaStream_t passed as void*, NULL = legacy default stream) and return a status
  * code; no C++ exception crosses this boundary.  A circuit handle is immutable after
  * creation and may be used from several threads and streams at once.
@@ -144,6 +145,15 @@ int sqg_decompose_batched(const sqg_circuit* circuit, const void* targets_dev, i
                           int cost_variant, double* x_dev, double* cost_dev, int* calls_dev, double tolerance,
                           int max_calls, int max_outer, int iteration_loops, int stop_at_tolerance,
                           unsigned long long seed, void* workspace_dev, size_t workspace_bytes, void* stream);
+
+/* Measures the FP64 FMA peak of the current device in TFLOP/s (an FMA counts 2 flops) with
+ * independent DFMA chains on 8 CTAs per SM, timed with CUDA events; scratch_dev receives
+ * the chains' results (sqg_probe_fp64_scratch_bytes() bytes).  With active_lanes < 32 only
+ * that many lanes of each warp compute while the rate is still reported for full warps,
+ * which shows how the FP64 pipe charges partially active warps.  The roofline denominator
+ * of the FP64-bound kernels.  No counterpart in the reference (measurement utility). */
+size_t sqg_probe_fp64_scratch_bytes(void);
+int sqg_probe_fp64_tflops(double* tflops, int active_lanes, void* scratch_dev, size_t scratch_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -17,7 +17,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 LIB_PATH = os.path.join(PKG_DIR, "libsqg.so")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-CU_SOURCES = ["engine.cu", "decompose.cu"]
+CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -106,6 +106,9 @@ def _declare(lib):
     lib.sqg_apply.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_ll, c_int, vp, c_sz, vp]
     lib.sqg_apply_from_right.argtypes = [vp, vp, vp, c_int, c_ll, vp, c_sz, vp]
     lib.sqg_combined_unitary.argtypes = [vp, vp, vp, c_int, vp, vp, c_sz, vp]
+    lib.sqg_probe_fp64_scratch_bytes.restype = c_sz
+    lib.sqg_probe_fp64_scratch_bytes.argtypes = []
+    lib.sqg_probe_fp64_tflops.argtypes = [ctypes.POINTER(ctypes.c_double), c_int, vp, c_sz, vp]
     lib.sqg_decompose_workspace_bytes.restype = c_sz
     lib.sqg_decompose_workspace_bytes.argtypes = [vp, c_int, c_int]
     lib.sqg_decompose_batched.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, ctypes.c_double, c_int,
@@ -126,6 +129,20 @@ def lib():
     return _lib
 
 
+def probe_fp64_tflops(active_lanes=32):
+    """Live FP64 FMA peak of the current CUDA device (TFLOP/s)."""
+    from . import _device as dev
+
+    dev.require_cuda()
+    l = lib()
+    nbytes = l.sqg_probe_fp64_scratch_bytes()
+    buf = dev.torch.empty(nbytes, dtype=dev.torch.uint8, device="cuda")
+    out = ctypes.c_double()
+    check(l.sqg_probe_fp64_tflops(ctypes.byref(out), int(active_lanes), buf.data_ptr(), nbytes, dev.stream_ptr()),
+          "sqg_probe_fp64_tflops")
+    return out.value
+
+
 def check(status, what=""):
     if status != SQG_OK:
         msg = lib().sqg_last_error().decode(errors="replace")
@@ -137,4 +154,5 @@ EXPORTED_SYMBOLS = [
     "sqg_circuit_qbit_num", "sqg_circuit_gate_num", "sqg_cost_grad_workspace_bytes",
     "sqg_cost_grad_checkpoint_workspace_bytes", "sqg_cost_grad", "sqg_apply_workspace_bytes", "sqg_apply",
     "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched",
+    "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
 ]
