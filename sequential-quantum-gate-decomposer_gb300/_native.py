@@ -21,8 +21,10 @@ CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
-# status codes (sqg.h)
+# status codes and limits (sqg.h)
 SQG_OK = 0
+SQG_ERR_WORKSPACE = 3
+SQG_NOALLOC_SCRATCH_BYTES = 32 << 20
 STATUS_TEXT = {0: "ok", 1: "invalid argument", 2: "unsupported configuration", 3: "workspace too small",
                4: "CUDA error", 5: "wrong number of parameters"}
 
@@ -101,6 +103,7 @@ def _declare(lib):
     lib.sqg_cost_grad_checkpoint_workspace_bytes.restype = c_sz
     lib.sqg_cost_grad_checkpoint_workspace_bytes.argtypes = [vp, c_int, c_int, c_int]
     lib.sqg_cost_grad.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_int, c_int, vp, vp, c_int, vp, c_sz, vp]
+    lib.sqg_cost_grad_noalloc.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_int, c_int, vp, vp, c_int, vp]
     lib.sqg_apply_workspace_bytes.restype = c_sz
     lib.sqg_apply_workspace_bytes.argtypes = [vp, c_int]
     lib.sqg_apply.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_ll, c_int, vp, c_sz, vp]
@@ -152,7 +155,8 @@ def check(status, what=""):
 EXPORTED_SYMBOLS = [
     "sqg_status_string", "sqg_last_error", "sqg_circuit_create", "sqg_circuit_destroy", "sqg_circuit_param_num",
     "sqg_circuit_qbit_num", "sqg_circuit_gate_num", "sqg_cost_grad_workspace_bytes",
-    "sqg_cost_grad_checkpoint_workspace_bytes", "sqg_cost_grad", "sqg_apply_workspace_bytes", "sqg_apply",
+    "sqg_cost_grad_checkpoint_workspace_bytes", "sqg_cost_grad", "sqg_cost_grad_noalloc", "sqg_apply_workspace_bytes",
+    "sqg_apply",
     "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched",
     "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
 ]

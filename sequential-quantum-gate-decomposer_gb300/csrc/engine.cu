@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -588,6 +589,58 @@ int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* 
   dim3 fgrid(B, with_grad ? (c->P + 127) / 128 : 1);
   k_finish<<<fgrid, 128, 0, s>>>(wtr, wgr, l.plan.tiles, c->P, cols, variant, cost, with_grad ? grad : nullptr);
   return cuda_status(cudaGetLastError(), "k_finish");
+}
+
+}  // extern "C"
+
+// ---- allocation-free cost/gradient ---------------------------------------------------
+// The scratch of sqg_cost_grad_noalloc: a file-scope device array of fixed size.  Host
+// code must not take its address directly (that is a host-side stand-in); the device
+// address is looked up once per device with cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SQG_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoallocMaxDevices] = {};
+
+int noalloc_scratch(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kNoallocMaxDevices) return fail(SQG_ERR_UNSUPPORTED, "device ordinal beyond 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(no-alloc scratch)");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return SQG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int sqg_cost_grad_noalloc(const sqg_circuit* c, const double* theta, int B, const void* target, int cols,
+                          long long target_batch_stride, int trace_offset, int variant, double* cost, double* grad,
+                          int checkpoint_interval, void* stream) {
+  int st = check_circuit(c);
+  if (st) return st;
+  if (B <= 0 || cols <= 0 || checkpoint_interval < 0)
+    return fail(SQG_ERR_INVALID_ARGUMENT, "bad batch, target width or checkpoint interval");
+  const bool with_grad = grad != nullptr && c->P > 0;
+  const size_t need = eval_layout(c, B, cols, with_grad, with_grad ? checkpoint_interval : 0).end;
+  if (need > SQG_NOALLOC_SCRATCH_BYTES)
+    return fail(SQG_ERR_WORKSPACE, "sqg_cost_grad_noalloc: this call needs " + std::to_string(need) +
+                                       " bytes of scratch but the built-in array holds " +
+                                       std::to_string((size_t)SQG_NOALLOC_SCRATCH_BYTES) +
+                                       "; use sqg_cost_grad with a caller-allocated workspace or a smaller batch");
+  void* ws = nullptr;
+  if ((st = noalloc_scratch(&ws))) return st;
+  return sqg_cost_grad(c, theta, B, target, cols, target_batch_stride, trace_offset, variant, cost, grad,
+                       checkpoint_interval, ws, SQG_NOALLOC_SCRATCH_BYTES, stream);
 }
 
 size_t sqg_apply_workspace_bytes(const sqg_circuit* c, int batch) {
