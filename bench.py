@@ -104,8 +104,7 @@ def make_workload(sqg, wl, orc_matrix=None, seed=1234):
     rng = np.random.default_rng(seed)
     ansatz = wl.cnot_u3_ansatz(3, ANSATZ_BLOCKS)
     if orc_matrix is None:
-        def orc_matrix(circ, theta):
-            return circ.get_Matrix(theta)
+        orc_matrix = wl.circuit_matrix
     U = wl.three_qubit_targets(N_TARGETS, rng, orc_matrix)
     targets = np.ascontiguousarray(np.conj(np.transpose(U, (0, 2, 1))))
     return ansatz, targets

@@ -176,6 +176,32 @@ int sqg_decompose_batched(const sqg_circuit* circuit, const void* targets_dev, i
 size_t sqg_probe_fp64_scratch_bytes(void);
 int sqg_probe_fp64_tflops(double* tflops, int active_lanes, void* scratch_dev, size_t scratch_bytes, void* stream);
 
+/* ---- Learned initialiser kernels (BF16 operands, FP32 accumulation) --------------------
+ * The initialiser maps a target to starting angles; it has no counterpart in the reference
+ * (SQUANDER starts from zeros, random or close-to-zero angles, Decomposition_Base.cpp:415-436),
+ * and only proposes start points to the decomposition kernels.  All pointers are device
+ * pointers; bf16 buffers are `void*` holding IEEE bfloat16. */
+/* C[M][N] = sum_k A'[m][k] B'[k][n] (+ bias[n]) (ReLU if relu) (+ C if accumulate), written as
+ * fp32 to C and/or bf16 to C_bf16 (row stride N both).  A' = A (M x K, row stride lda) or A^T
+ * (A stored K x M) when transA; B' = B (K x N, row stride ldb) or B^T (B stored N x K). */
+int sqg_mlp_gemm_bf16(int M, int N, int K, const void* A, int lda, int transA, const void* B, int ldb, int transB,
+                      float* C, int ldc, const float* bias, int relu, void* C_bf16, int accumulate, void* stream);
+int sqg_mlp_to_bf16(const float* x, void* y_bf16, long long n, void* stream);
+/* dA <- dA * (Z > 0) in place, with a bf16 copy. */
+int sqg_mlp_relu_backward(float* dA, const float* Z, void* dZ_bf16, long long n, void* stream);
+/* db[n] = sum_m dZ[m][n]. */
+int sqg_mlp_col_sum(const float* dZ, int M, int N, float* db, void* stream);
+/* Adam step (bias-corrected, step >= 1) on fp32 weights; refreshes w_bf16 when non-null. */
+int sqg_mlp_adam(float* w, const float* g, float* m, float* v, void* w_bf16, long long n, float lr, float beta1,
+                 float beta2, float eps, int step, float weight_decay, void* stream);
+/* Angle head: out is M x 2P (cos, sin) pairs; theta = atan2.  mode 0: angles only; mode 1:
+ * supervised loss against target angles (loss_rows, out_grad); mode 2: out_grad = chain
+ * rule of dL/dtheta through atan2.  Gradients are multiplied by scale. */
+int sqg_mlp_angle_head(const float* out, int M, int P, double* theta, const double* target_or_dtheta, int mode,
+                       float scale, float* out_grad, float* loss_rows, void* stream);
+/* Network input: interleaved Re/Im of n_complex complex128 values as bf16. */
+int sqg_mlp_features(const void* U, long long n_complex, void* x_bf16, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,7 +17,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 LIB_PATH = os.path.join(PKG_DIR, "libsqg.so")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu"]
+CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu", "mlp.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -159,4 +159,6 @@ EXPORTED_SYMBOLS = [
     "sqg_apply",
     "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched",
     "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
+    "sqg_mlp_gemm_bf16", "sqg_mlp_to_bf16", "sqg_mlp_relu_backward", "sqg_mlp_col_sum", "sqg_mlp_adam",
+    "sqg_mlp_angle_head", "sqg_mlp_features",
 ]

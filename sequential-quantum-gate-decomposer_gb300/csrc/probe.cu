@@ -9,14 +9,15 @@
 
 namespace {
 
-__global__ void k_fp64_peak(double* out, int iters, int active_lanes) {
+__global__ void k_fp64_peak(double* out, int iters, int active_lanes, double a, double b) {
   double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
          x7 = x0 + 7;
-  const double a = 0.9999999, b = 1e-7;
-  if ((int)(threadIdx.x & 31) < active_lanes)
+  if ((int)(threadIdx.x & 31) < active_lanes) {
+#pragma unroll 4
   for (int i = 0; i < iters; i++) {
     x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
     x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
@@ -44,9 +45,9 @@ extern "C" int sqg_probe_fp64_tflops(double* tflops, int active_lanes, void* scr
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  k_fp64_peak<<<blocks, threads, 0, s>>>((double*)scratch, iters, active_lanes);  // warm-up
+  k_fp64_peak<<<blocks, threads, 0, s>>>((double*)scratch, iters, active_lanes, 0.9999999, 1e-7);  // warm-up
   cudaEventRecord(e0, s);
-  k_fp64_peak<<<blocks, threads, 0, s>>>((double*)scratch, iters, active_lanes);
+  k_fp64_peak<<<blocks, threads, 0, s>>>((double*)scratch, iters, active_lanes, 0.9999999, 1e-7);
   cudaEventRecord(e1, s);
   cudaError_t e = cudaEventSynchronize(e1);
   float ms = 0.f;

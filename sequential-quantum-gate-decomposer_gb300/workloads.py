@@ -70,6 +70,46 @@ def random_gate_circuit(n, gates, rng):
     return c
 
 
+def _one_qubit(t, p, ps):
+    if t == 7:  # U3 (theta/2, phi, lambda)
+        c, s = np.cos(p[ps]), np.sin(p[ps])
+        ep, el = np.exp(1j * p[ps + 1]), np.exp(1j * p[ps + 2])
+        return np.array([[c, -el * s], [ep * s, ep * el * c]])
+    c, s = np.cos(p[ps]), np.sin(p[ps])
+    if t == 9:  # RX
+        return np.array([[c, -1j * s], [-1j * s, c]])
+    if t == 10:  # RZ
+        return np.diag([c - 1j * s, c + 1j * s])
+    return np.array([[c, -s], [s, c]], dtype=complex)  # RY, CRY
+
+
+def circuit_matrix(circuit, theta):
+    """Dense matrix of a small circuit (n <= 8) on the host, for building synthetic targets
+    without a device round trip per target."""
+    n = circuit.qbit_num
+    N = 1 << n
+    p = np.asarray(theta, dtype=np.float64)
+    M = np.eye(N, dtype=complex)
+    idx = np.arange(N)
+    for t, tg, ctl, ps in circuit.gate_records():
+        t, tg, ctl, ps = int(t), int(tg), int(ctl), int(ps)
+        lo = idx[((idx >> tg) & 1) == 0]
+        if ctl >= 0:
+            lo = lo[((lo >> ctl) & 1) == 1]
+        hi = lo | (1 << tg)
+        if t == 5:  # CNOT
+            M[[lo, hi]] = M[[hi, lo]]
+            continue
+        if t == 4:  # CZ
+            M[hi] = -M[hi]
+            continue
+        g = _one_qubit(t, p, ps)
+        x, y = M[lo].copy(), M[hi].copy()
+        M[lo] = g[0, 0] * x + g[0, 1] * y
+        M[hi] = g[1, 0] * x + g[1, 1] * y
+    return M
+
+
 def random_angles(P, rng, size=None):
     shape = (P,) if size is None else (size, P)
     return rng.uniform(0.0, 2 * np.pi, shape)
@@ -88,3 +128,61 @@ def three_qubit_targets(count, rng, matrix_fn):
         c = cnot_u3_ansatz(3, k, pairs="random", rng=rng)
         out[i] = matrix_fn(c, random_angles(c.get_Parameter_Num(), rng))
     return out
+
+
+def _u3_batch(p):
+    """(S, 3) stored U3 parameters -> (S, 2, 2) matrices."""
+    c, s = np.cos(p[:, 0]), np.sin(p[:, 0])
+    ep, el = np.exp(1j * p[:, 1]), np.exp(1j * p[:, 2])
+    g = np.empty((p.shape[0], 2, 2), dtype=complex)
+    g[:, 0, 0], g[:, 0, 1], g[:, 1, 0], g[:, 1, 1] = c, -el * s, ep * s, ep * el * c
+    return g
+
+
+def _embed_batch(g, q, n):
+    """Per-instance one-qubit gates g (S, 2, 2) on qubits q (S,) -> (S, 2^n, 2^n)."""
+    S, N = g.shape[0], 1 << n
+    idx = np.arange(N)
+    bit = (idx[None, :] >> q[:, None]) & 1                      # (S, N)
+    partner = idx[None, :] ^ (1 << q[:, None])                  # (S, N)
+    M = np.zeros((S, N, N), dtype=complex)
+    rows = np.arange(S)[:, None]
+    M[rows, idx[None, :], idx[None, :]] = g[rows, bit, bit]
+    M[rows, idx[None, :], partner] = g[rows, bit, 1 - bit]
+    return M
+
+
+def random_circuit_targets(count, n, rng, max_blocks=14):
+    """Vectorised generator of products of random CNOT+U3 circuits: U3 on every qubit, then
+    k ~ U{1..max_blocks} blocks of [CNOT(c, t), U3(c), U3(t)] with (c, t) uniform over
+    ordered pairs and U3 angles U[0, 2 pi).  Returns (count, 2^n, 2^n) matrices U."""
+    N = 1 << n
+    U = np.broadcast_to(np.eye(N, dtype=complex), (count, N, N)).copy()
+    for q in range(n):
+        g = _u3_batch(rng.uniform(0, 2 * np.pi, (count, 3)))
+        U = _embed_batch(g, np.full(count, q), n) @ U
+    k = rng.integers(1, max_blocks + 1, count)
+    pairs = np.array([(a, b) for a in range(n) for b in range(n) if a != b])
+    idx = np.arange(N)
+    for blk in range(max_blocks):
+        act = k > blk
+        if not act.any():
+            break
+        sel = pairs[rng.integers(len(pairs), size=count)]
+        ctl, tgt = sel[:, 0], sel[:, 1]
+        # CNOT as a row permutation: rows with the control bit set swap across the target bit
+        src = np.where(((idx[None, :] >> ctl[:, None]) & 1) == 1, idx[None, :] ^ (1 << tgt[:, None]), idx[None, :])
+        Up = np.take_along_axis(U, src[:, :, None], axis=1)
+        g1 = _embed_batch(_u3_batch(rng.uniform(0, 2 * np.pi, (count, 3))), ctl, n)
+        g2 = _embed_batch(_u3_batch(rng.uniform(0, 2 * np.pi, (count, 3))), tgt, n)
+        Up = g2 @ (g1 @ Up)
+        U = np.where(act[:, None, None], Up, U)
+    return U
+
+
+def haar_unitaries(count, dim, rng):
+    a = rng.standard_normal((count, dim, dim)) + 1j * rng.standard_normal((count, dim, dim))
+    q, r = np.linalg.qr(a)
+    d = np.diagonal(r, axis1=1, axis2=2)
+    phase = np.where(np.abs(d) > 0, d / np.abs(d), 1.0)
+    return np.ascontiguousarray(q * phase[:, None, :], dtype=np.complex128)
