@@ -121,6 +121,27 @@ int sqg_cost_grad_noalloc(const sqg_circuit* circuit, const double* theta_dev, i
                           int cols, long long target_batch_stride, int trace_offset, int cost_variant,
                           double* cost_dev, double* grad_dev, int checkpoint_interval, void* stream);
 
+/* ---- Ragged batches: instances with different circuits (qubit counts) in one launch ----
+ * Plans the evaluation of `count` instances, instance i with circuits[i] (its own qubit
+ * count, gates and parameters) against its own 2^n_i x cols[i] target.  Parameters,
+ * targets and gradients are packed flat in instance order; sqg_ragged_layout returns the
+ * count+1 offsets (in doubles for parameters/gradients, complex elements for targets).
+ * tile_cols (optional, per instance, 0 = automatic) fixes the column-tile width, for
+ * autotuning.  The launch is a persistent grid pulling (instance, tile) work items from a
+ * queue ordered by decreasing work; kernel attributes are set at planning time, so the
+ * calls of sqg_ragged_cost_grad can be captured in a CUDA graph.  Replaces the reference's
+ * per-instance loop of Optimization_Interface::optimization_problem_batched
+ * (Optimization_Interface.cpp:940-1033), which requires one shared circuit. */
+typedef struct sqg_ragged_batch sqg_ragged_batch;
+int sqg_ragged_create(const sqg_circuit* const* circuits, const int* cols, int count, int with_grad,
+                      const int* tile_cols, sqg_ragged_batch** out);
+int sqg_ragged_destroy(sqg_ragged_batch* batch);
+size_t sqg_ragged_workspace_bytes(const sqg_ragged_batch* batch);
+int sqg_ragged_layout(const sqg_ragged_batch* batch, long long* theta_offsets, long long* target_offsets);
+int sqg_ragged_cost_grad(const sqg_ragged_batch* batch, const double* theta_dev, const void* targets_dev,
+                         int cost_variant, double* cost_dev, double* grad_dev, void* workspace_dev,
+                         size_t workspace_bytes, void* stream);
+
 /* Workspace bytes needed by sqg_apply. */
 size_t sqg_apply_workspace_bytes(const sqg_circuit* circuit, int batch);
 

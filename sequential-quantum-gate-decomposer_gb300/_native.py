@@ -17,7 +17,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 LIB_PATH = os.path.join(PKG_DIR, "libsqg.so")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu", "mlp.cu"]
+CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu", "mlp.cu", "ragged.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -104,6 +104,12 @@ def _declare(lib):
     lib.sqg_cost_grad_checkpoint_workspace_bytes.argtypes = [vp, c_int, c_int, c_int]
     lib.sqg_cost_grad.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_int, c_int, vp, vp, c_int, vp, c_sz, vp]
     lib.sqg_cost_grad_noalloc.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_int, c_int, vp, vp, c_int, vp]
+    lib.sqg_ragged_create.argtypes = [vp, vp, c_int, c_int, vp, ctypes.POINTER(vp)]
+    lib.sqg_ragged_destroy.argtypes = [vp]
+    lib.sqg_ragged_workspace_bytes.restype = c_sz
+    lib.sqg_ragged_workspace_bytes.argtypes = [vp]
+    lib.sqg_ragged_layout.argtypes = [vp, vp, vp]
+    lib.sqg_ragged_cost_grad.argtypes = [vp, vp, vp, c_int, vp, vp, vp, c_sz, vp]
     lib.sqg_apply_workspace_bytes.restype = c_sz
     lib.sqg_apply_workspace_bytes.argtypes = [vp, c_int]
     lib.sqg_apply.argtypes = [vp, vp, c_int, vp, c_int, c_ll, c_ll, c_int, vp, c_sz, vp]
@@ -161,4 +167,6 @@ EXPORTED_SYMBOLS = [
     "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
     "sqg_mlp_gemm_bf16", "sqg_mlp_to_bf16", "sqg_mlp_relu_backward", "sqg_mlp_col_sum", "sqg_mlp_adam",
     "sqg_mlp_angle_head", "sqg_mlp_features",
+    "sqg_ragged_create", "sqg_ragged_destroy", "sqg_ragged_workspace_bytes", "sqg_ragged_layout",
+    "sqg_ragged_cost_grad",
 ]
