@@ -433,7 +433,13 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.seed = seed;
   a.zglob = (double*)workspace;
   a.z_in_smem = zs ? 1 : 0;
-  cudaError_t e = cudaFuncSetAttribute(k_decompose, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess && smem > (size_t)optin)
+    return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
+  // raised to the device maximum, never lowered: the attribute is shared by all callers
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_decompose, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
   // one thread per parameter for the vector and Z-matrix work, at least two warps
   const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));

@@ -249,10 +249,16 @@ TilePlan plan_tiles(int N, int cols, bool grad) {
   return pl;
 }
 
+// Raises a kernel's dynamic shared memory limit to the device's opt-in maximum (never
+// lowers it: the attribute is shared by every caller of the kernel).
 template <typename K>
 int set_smem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess && bytes > (size_t)optin) return fail(SQG_ERR_UNSUPPORTED, "tile exceeds shared memory");
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
   }
   return SQG_OK;

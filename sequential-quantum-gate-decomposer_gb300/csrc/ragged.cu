@@ -268,11 +268,19 @@ int sqg_ragged_create(const sqg_circuit* const* circuits, const int* cols, int c
     e = cudaMemcpy(r->d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !gate_map.empty())
     e = cudaMemcpy(r->d_gate_map, gate_map.data(), sizeof(int2) * gate_map.size(), cudaMemcpyHostToDevice);
-  // kernel attributes are set here, once, so that launches can be captured in CUDA graphs
+  // kernel attributes are set here, at planning time and to the device's opt-in maximum
+  // (the attribute is per kernel, shared by every batch), so that launches can be captured
+  // in CUDA graphs
+  int optin = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, r->device);
+  if (e == cudaSuccess && smem + 64 > (size_t)optin) {
+    free_batch(r);
+    return set_error(SQG_ERR_UNSUPPORTED, "work item does not fit in shared memory");
+  }
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_ragged_tiles<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_ragged_tiles<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 64);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_ragged_tiles<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_ragged_tiles<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 64);
   int per_sm = 0, sms = 0;
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
