@@ -225,6 +225,8 @@ def bench_ours(args):
         line["gate_apply_n12"] = bench_gate_apply(sqg, wl, torch)
         line["cost_grad_n8"] = bench_cost_grad(sqg, wl, torch)
         line["cost_grad_uneven"] = bench_ragged(sqg, wl, torch)
+        line["cost_grad_n10"] = bench_cost_grad_n10(sqg, wl, torch)
+        line["decompose_n4_single"] = bench_single_n4(sqg, wl, torch)
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(sqg, wl, ansatz, targets, P, budget_s=args.cpu_seconds)
     return line
@@ -272,6 +274,18 @@ def bench_gate_apply(sqg, wl, torch):
     res["fused"]["fp64_frac"] = res["fused"]["fp64_tflops"] / FP64_PEAK_TFLOPS
     res["unfused"]["hbm_frac"] = res["unfused"]["algorithmic_GBps"] / hbm
     res["unfused"]["fp64_tflops"] = 2.0 * B * fwd_ops / res["unfused"]["seconds"] / 1e12
+    # one full cost + adjoint-gradient evaluation of the same circuit at n = 12
+    ev = sqg.CostEvaluator(c, torch.eye(N, dtype=torch.complex128, device="cuda"))
+    ev.cost_grad(th[:1])
+    torch.cuda.synchronize()
+    e0.record()
+    ev.cost_grad(th[:1])
+    e1.record()
+    e1.synchronize()
+    tg = e0.elapsed_time(e1) / 1e3
+    gops = fp64_ops_per_eval(recs, N, N)
+    res["cost_grad_eval"] = {"seconds": tg, "fp64_tflops": 2.0 * gops / tg / 1e12}
+    del ev
     res["peak_hbm_GBps"] = hbm
     res["peak_source"] = src
     res["config"] = "n=12 (4096x4096 complex128), 2000 random gates U3/RY/CNOT/CZ/CRY, batch 4"
@@ -336,6 +350,64 @@ def bench_ragged(sqg, wl, torch):
             "fp64_tflops": 2.0 * ops / t / 1e12, "fp64_frac": 2.0 * ops / t / 1e12 / FP64_PEAK_TFLOPS,
             "tile_cols_by_n": {int(n): int(choice[[c.qbit_num for c in circs].index(n)]) for n in range(3, 10)
                                if n in [c.qbit_num for c in circs]}}
+
+
+def bench_single_n4(sqg, wl, torch):
+    """BASELINE config 1: one 4-qubit Haar target, U3 layer + 40 nearest-neighbour CNOT
+    blocks (P = 252), BFGS towards cost < 1e-8 through the drop-in class (host BFGS, one
+    GPU cost+gradient call per evaluation) and through the device decomposer (B = 1)."""
+    rng = np.random.default_rng(11)
+    U = wl.haar_unitary(16, rng)
+    c = wl.cnot_u3_ansatz(4, 40)
+    P = c.get_Parameter_Num()
+    x0 = rng.uniform(0, 2 * np.pi, P)
+    d = sqg.N_Qubit_Decomposition_custom(U.conj().T, config={"optimization_tolerance": 1e-8, "max_outer_iterations": 1,
+                                                             "max_inner_iterations": 2000})
+    d.set_Gate_Structure(c)
+    d.set_Optimized_Parameters(x0)
+    t0 = time.perf_counter()
+    d.Start_Decomposition()
+    t_host = time.perf_counter() - t0
+    host_calls = d.get_Num_of_Iters()
+    bd = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=2000, max_outer=1)
+    tdev = torch.from_numpy(np.ascontiguousarray(U.conj().T)[None]).cuda()
+    bd.run(tdev, x0[None])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x, cost, calls = bd.run(tdev, x0[None])
+    torch.cuda.synchronize()
+    t_dev = time.perf_counter() - t0
+    return {"config": "n=4 Haar target, 40 NN CNOT+U3 blocks (P=252), one BFGS run of at most 2000 evaluations",
+            "host_bfgs": {"evals": host_calls, "seconds": t_host, "evals_per_s": host_calls / t_host,
+                          "final_cost": d.get_Decomposition_Error()},
+            "device_bfgs": {"evals": int(calls.item()), "seconds": t_dev, "evals_per_s": int(calls.item()) / t_dev,
+                            "final_cost": float(cost.item())},
+            "note": "40 CNOTs are below the 61-CNOT lower bound for generic 4-qubit unitaries, so the cost "
+                    "cannot reach 1e-8 on a Haar target"}
+
+
+def bench_cost_grad_n10(sqg, wl, torch):
+    """BASELINE config 3 shape: n = 10, 300 CNOT blocks over uniformly drawn ordered pairs
+    (P = 1830), cost + adjoint gradient of 64 parameter vectors, plain and checkpointed."""
+    rng = np.random.default_rng(12)
+    c = wl.cnot_u3_ansatz(10, 300, pairs="random", rng=rng)
+    P = c.get_Parameter_Num()
+    U = c.get_Matrix(rng.uniform(0, 2 * np.pi, P))
+    ev = sqg.CostEvaluator(c, np.ascontiguousarray(U.conj().T))
+    th = torch.from_numpy(rng.uniform(0, 2 * np.pi, (64, P))).cuda()
+    out = {"config": "n=10, 300 random-pair blocks (P=1830), B=64, cost + adjoint gradient"}
+    for ck in (0, 30):
+        ev.cost_grad(th[:2], checkpoint_interval=ck)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ev.cost_grad(th, checkpoint_interval=ck)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        ops = fp64_ops_per_eval(c.gate_records(), 1024, 1024) * 64
+        out["checkpoint_%d" % ck] = {"seconds": t, "evals_per_s": 64 / t, "fp64_tflops": 2.0 * ops / t / 1e12}
+    return out
 
 
 def cpu_baseline(sqg, wl, ansatz, targets, P, budget_s=20.0):
