@@ -173,7 +173,7 @@ int sqg_combined_unitary(const sqg_circuit* circuit, const double* theta_dev, co
  *   targets_dev  batch x rows x cols complex128 (each U^dagger);
  *   x_dev        batch x P doubles: start points in, best parameters out;
  *   cost_dev     batch doubles out (best cost);  calls_dev  batch ints out (cost+gradient
- *                evaluations used).
+ *                evaluations used);  iters_dev  batch ints out (BFGS iterations) or NULL.
  * Each instance runs up to max_outer outer iterations of iteration_loops BFGS runs of at
  * most max_calls evaluations, perturbing the best point by U[0, 2 pi)/100 after an
  * improvement, and stops once the best cost is below `tolerance`; with
@@ -184,7 +184,8 @@ int sqg_combined_unitary(const sqg_circuit* circuit, const double* theta_dev, co
  * The workspace holds the per-instance BFGS matrices when they do not fit on chip. */
 size_t sqg_decompose_workspace_bytes(const sqg_circuit* circuit, int batch, int cols);
 int sqg_decompose_batched(const sqg_circuit* circuit, const void* targets_dev, int cols, int batch, int trace_offset,
-                          int cost_variant, double* x_dev, double* cost_dev, int* calls_dev, double tolerance,
+                          int cost_variant, double* x_dev, double* cost_dev, int* calls_dev, int* iters_dev,
+                          double tolerance,
                           int max_calls, int max_outer, int iteration_loops, int stop_at_tolerance,
                           unsigned long long seed, void* workspace_dev, size_t workspace_bytes, void* stream);
 
@@ -222,6 +223,14 @@ int sqg_mlp_angle_head(const float* out, int M, int P, double* theta, const doub
                        float scale, float* out_grad, float* loss_rows, void* stream);
 /* Network input: interleaved Re/Im of n_complex complex128 values as bf16. */
 int sqg_mlp_features(const void* U, long long n_complex, void* x_bf16, void* stream);
+/* C[M][N] = A[M][K] B[N][K]^T (+ bias, ReLU) on the tcgen05 tensor cores (accumulator in
+ * TMEM, operands staged by TMA with 128-byte swizzle); A and B bf16 row-major (K-major),
+ * K, lda, ldb multiples of 8, 16-byte aligned.  Waits inside the kernel are bounded: a
+ * time-out writes a non-zero code to *err_dev (device int) instead of hanging. */
+int sqg_mlp_gemm_tc(int M, int N, int K, const void* A, int lda, const void* B, int ldb, float* C, int ldc,
+                    const float* bias, int relu, void* C_bf16, int* err_dev, void* stream);
+/* out[c][r] = in[r][c] for a rows x cols bf16 matrix. */
+int sqg_mlp_transpose_bf16(const void* in, int rows, int cols, int ld_in, void* out, int ld_out, void* stream);
 
 #ifdef __cplusplus
 }

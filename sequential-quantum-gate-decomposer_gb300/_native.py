@@ -17,7 +17,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 LIB_PATH = os.path.join(PKG_DIR, "libsqg.so")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu", "mlp.cu", "ragged.cu"]
+CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu", "mlp.cu", "ragged.cu", "gemm_tc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -120,8 +120,8 @@ def _declare(lib):
     lib.sqg_probe_fp64_tflops.argtypes = [ctypes.POINTER(ctypes.c_double), c_int, vp, c_sz, vp]
     lib.sqg_decompose_workspace_bytes.restype = c_sz
     lib.sqg_decompose_workspace_bytes.argtypes = [vp, c_int, c_int]
-    lib.sqg_decompose_batched.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, ctypes.c_double, c_int,
-                                          c_int, c_int, c_int, ctypes.c_ulonglong, vp, c_sz, vp]
+    lib.sqg_decompose_batched.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double,
+                                          c_int, c_int, c_int, c_int, ctypes.c_ulonglong, vp, c_sz, vp]
 
 
 def lib():
@@ -168,5 +168,5 @@ EXPORTED_SYMBOLS = [
     "sqg_mlp_gemm_bf16", "sqg_mlp_to_bf16", "sqg_mlp_relu_backward", "sqg_mlp_col_sum", "sqg_mlp_adam",
     "sqg_mlp_angle_head", "sqg_mlp_features",
     "sqg_ragged_create", "sqg_ragged_destroy", "sqg_ragged_workspace_bytes", "sqg_ragged_layout",
-    "sqg_ragged_cost_grad",
+    "sqg_ragged_cost_grad", "sqg_mlp_gemm_tc", "sqg_mlp_transpose_bf16",
 ]

@@ -33,7 +33,8 @@ class BatchedDecomposer:
 
     def run(self, targets_udag, x0, seed=0, stream=None):
         """targets_udag: (B, rows, cols) complex128; x0: (B, P) float64 (host or device).
-        Returns CUDA tensors (x (B, P), cost (B,), calls (B,) int32); asynchronous."""
+        Returns CUDA tensors (x (B, P), cost (B,), calls (B,) int32); asynchronous.  The BFGS
+        iteration counts of the call are left in self.iters."""
         t = dev.to_device_complex(targets_udag)
         if t.dim() != 3 or t.shape[1] != (1 << self.native.qbit_num):
             raise ValueError("targets must be (B, 2**qbit_num, cols)")
@@ -43,11 +44,12 @@ class BatchedDecomposer:
             raise ValueError("x0 must be (B, %d)" % self.native.param_num)
         cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
         calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
+        self.iters = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
         lib = _native.lib()
         ws = self._ws.get(lib.sqg_decompose_workspace_bytes(self.native.handle, B, cols))
         _native.check(lib.sqg_decompose_batched(
             self.native.handle, dev.ptr(t), cols, B, self.trace_offset, self.cost_variant, dev.ptr(x), dev.ptr(cost),
-            dev.ptr(calls), self.tolerance, self.max_calls, self.max_outer, self.iteration_loops,
+            dev.ptr(calls), dev.ptr(self.iters), self.tolerance, self.max_calls, self.max_outer, self.iteration_loops,
             1 if self.stop_at_tolerance else 0, int(seed) & 0xFFFFFFFFFFFFFFFF, dev.ptr(ws), ws.numel(),
             dev.stream_ptr(stream)), "sqg_decompose_batched")
         self._keep = t  # keep the target buffer alive until the caller synchronises

@@ -38,6 +38,7 @@ struct DecArgs {
   double* x;
   double* cost;
   int* calls;
+  int* iters;
   int B;
   double tol;
   int max_calls, max_outer, loops, early_stop;
@@ -207,7 +208,7 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
 }
 
 // BFGS_Powell::Optimize from sh.x (updated in place).  Returns the final cost.
-__device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls) {
+__device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, int& iters) {
   const int P = a.P;
   double* Z = sh.Z;
   for (int i = threadIdx.x; i < P * P; i += blockDim.x) Z[i] = (i % (P + 1)) == 0 ? 1.0 : 0.0;
@@ -243,6 +244,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls) {
     if (gn <= 1e-19 * 1e-19 || dg >= 0.0 || f >= fprev) break;
     fprev = f;
     if (calls >= a.max_calls) break;
+    iters++;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
       sh.x0[i] = sh.x[i];
       sh.g0[i] = sh.g[i];
@@ -330,14 +332,14 @@ __global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
   for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = a.x[(long long)b * P + i];
   __syncthreads();
   double best = INFINITY;
-  int calls = 0;
+  int calls = 0, iters = 0;
   unsigned long long ctr = a.seed * 0x2545F4914F6CDD1DULL + (unsigned long long)b * 0x9E3779B97F4A7C15ULL;
   bool done = false;
   for (int outer = 0; outer < a.max_outer && !done; outer++) {
     for (int loop = 0; loop < a.loops; loop++) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.guess[i];
       __syncthreads();
-      double f = dec_bfgs(a, sh, b, calls);
+      double f = dec_bfgs(a, sh, b, calls, iters);
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = sh.x[i];
       __syncthreads();
       if (f < best) {
@@ -362,6 +364,7 @@ __global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
   if (threadIdx.x == 0) {
     a.cost[b] = best;
     a.calls[b] = calls;
+    if (a.iters) a.iters[b] = iters;
   }
 }
 
@@ -400,7 +403,8 @@ size_t sqg_decompose_workspace_bytes(const sqg_circuit* c, int batch, int cols) 
 }
 
 int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, int batch, int trace_offset,
-                          int cost_variant, double* x, double* cost, int* calls, double tolerance, int max_calls,
+                          int cost_variant, double* x, double* cost, int* calls, int* iters, double tolerance,
+                          int max_calls,
                           int max_outer, int iteration_loops, int stop_at_tolerance, unsigned long long seed,
                           void* workspace, size_t ws_bytes, void* stream) {
   if (!c || !targets || !x || !cost || !calls || batch <= 0 || batch > 0x7fffffff / 2 || cols <= 0 || cols > c->N)
@@ -425,7 +429,7 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.variant = cost_variant;
   a.targets = (const double2*)targets;
   a.tstride = (long long)c->N * cols;
-  a.x = x; a.cost = cost; a.calls = calls;
+  a.x = x; a.cost = cost; a.calls = calls; a.iters = iters;
   a.B = batch;
   a.tol = tolerance;
   a.max_calls = max_calls; a.max_outer = max_outer; a.loops = iteration_loops;
