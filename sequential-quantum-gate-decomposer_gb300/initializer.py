@@ -145,6 +145,7 @@ class MLP:
                 if not last:
                     self._gemm(a, False, self.Wb[i], True, M, fan_out, fan_in, Cb=ab, bias=self.b[i], relu=True,
                                lda=fan_in, ldb=fan_in)
+            if not last:
                 acts.append(ab)
                 a = ab
             pre.append(z)
