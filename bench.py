@@ -141,6 +141,43 @@ def fp64_ops_per_bfgs_iteration(P):
     return int(10.5 * P * P + 30 * P)
 
 
+def bench_learned(sqg, wl, torch, ansatz, targets, tdev, plain_rate, plain_solved, steps):
+    """Learned path: the MLP initialiser (trained here on GPU-generated decompositions of
+    131072 synthetic targets, supervised, tcgen05 GEMMs) proposes the start points; each
+    timed step = network inference + the batched decomposition of the same 4096 targets."""
+    ini = importlib.import_module(PKG + ".initializer")
+    init, st = ini.train_initializer(ansatz, n_samples=131072, epochs=8, seed=4242)
+    P = ansatz.get_Parameter_Num()
+    dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=MAX_CALLS, max_outer=MAX_OUTER)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    dec.run(tdev, init.predict(tdev), seed=1)
+    torch.cuda.synchronize()
+    times, solved, calls_tot = [], 0, 0
+    for k in range(steps):
+        flush.add_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        x0 = init.predict(tdev)
+        x, cost, calls = dec.run(tdev, x0, seed=3000 + k)
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        solved += int((cost.cpu().numpy() < TOL).sum())
+        calls_tot += int(calls.cpu().numpy().astype(np.int64).sum())
+    init.mlp.check_errors()
+    # end to end: host targets in, host parameters and costs out
+    t0 = time.perf_counter()
+    T = torch.from_numpy(targets).cuda()
+    x, cost, calls = dec.run(T, init.predict(T), seed=4000)
+    xh, ch = x.cpu().numpy(), cost.cpu().numpy()
+    t_e2e = time.perf_counter() - t0
+    rate = solved / sum(times)
+    return {"value": rate, "ms_per_step": 1e3 * sum(times) / steps, "solved_fraction": solved / (N_TARGETS * steps),
+            "evaluations_per_step": calls_tot / steps, "e2e_value": int((ch < TOL).sum()) / t_e2e,
+            "ratio_vs_plain": rate / plain_rate, "training": st,
+            "init": "MLP 128 -> 4x1024 -> 186 (BF16, FP32 accumulate, tcgen05), trained on 131072 decompositions"}
+
+
 def bench_ours(args):
     import torch
 
@@ -228,6 +265,21 @@ def bench_ours(args):
                              "model FP64 ops of the evaluations and BFGS iterations performed"},
         "bfgs_iterations_per_step": iters_tot / args.steps,
     }
+    if not args.skip_learned:
+        lp = bench_learned(sqg, wl, torch, ansatz, targets, tdev, value, solved, args.steps)
+        line["plain"] = {"value": value, "ms_per_step": line["ms_per_step"], "solved_fraction": line["solved_fraction"],
+                         "evaluations_per_step": line["evaluations_per_step"], "e2e_value": e2e_value}
+        line["learned"] = lp
+        # the headline is the better of the two paths (the learned initialiser is part of the
+        # method); both are reported
+        if lp["value"] > value:
+            line["value"] = lp["value"]
+            line["ms_per_step"] = lp["ms_per_step"]
+            line["solved_fraction"] = lp["solved_fraction"]
+            line["evaluations_per_step"] = lp["evaluations_per_step"]
+            line["e2e"]["value"] = lp["e2e_value"]
+            line["config"]["init"] = "learned MLP initialiser (random-start plain path in 'plain')"
+            line["gpu_launches"] = args.steps * 12  # features, 9 GEMMs, angle head, decomposition
     if clk:
         line["clocks"] = clk
     if not args.skip_secondary:
@@ -528,6 +580,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-secondary", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-learned", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--ref-targets", type=int, default=32)
     args = ap.parse_args()
