@@ -560,6 +560,25 @@ def profile_case(case):
         m = torch.zeros((1, 4096, 4096), dtype=torch.complex128, device="cuda")
         c.apply_to_device(th, m, fused=True)
         c.apply_to_device(th, m, fused=False)
+    elif case == "mlp_gemm":
+        ini = importlib.import_module(PKG + ".initializer")
+        net = ini.MLP([8, 8], use_tc=True)
+        A = torch.randn((4096, 1024), device="cuda").to(torch.bfloat16)
+        B = torch.randn((1024, 1024), device="cuda").to(torch.bfloat16)
+        C = torch.empty((4096, 1024), dtype=torch.float32, device="cuda")
+        for _ in range(3):
+            net._tc(A, B, 4096, 1024, 1024, C=C)
+        torch.cuda.synchronize()
+        net.check_errors()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(20):
+            net._tc(A, B, 4096, 1024, 1024, C=C)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 20 / 1e3
+        print(json.dumps({"mlp_gemm_tc": {"M": 4096, "N": 1024, "K": 1024, "seconds": t,
+                                          "tflops": 2.0 * 4096 * 1024 * 1024 / t / 1e12}}))
     elif case == "cost_grad":
         c = wl.cnot_u3_ansatz(8, 60)
         P = c.get_Parameter_Num()
@@ -573,7 +592,7 @@ def profile_case(case):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe-fp64", action="store_true", help="print the live FP64 FMA peak by active lanes")
-    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad"], default=None)
+    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad", "mlp_gemm"], default=None)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
