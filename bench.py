@@ -627,12 +627,15 @@ def main():
         args.skip_secondary = True
         args.skip_cpu = rank != 0
         line = bench_ours(args)
+        # max step time over ranks, sum of solved targets over ranks (each rank decomposes its
+        # own 4096 targets: weak scaling, no collective on the data path)
         t = torch.tensor([line["ms_per_step"]], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        solved = torch.tensor([line["solved_fraction"] * N_TARGETS * args.steps], device="cuda", dtype=torch.float64)
+        dist.all_reduce(solved, op=dist.ReduceOp.SUM)
         if rank == 0:
             line["ms_per_step"] = float(t.item())
-            line["value"] = line["value"] * world * 0 + (line["solved_fraction"] * N_TARGETS * world) / (
-                line["ms_per_step"] / 1e3)
+            line["value"] = float(solved.item()) / (args.steps * line["ms_per_step"] / 1e3)
             line["n_gpus"] = world
             print(json.dumps(line))
         dist.destroy_process_group()
