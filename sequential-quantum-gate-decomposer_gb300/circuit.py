@@ -200,6 +200,24 @@ class Circuit:
         self.apply_to_device(params, m)
         view[...] = m.cpu().numpy()
 
+    def apply_to_list(self, inputs, parameters_mtx, parallel=1, is_f32=False):
+        """Applies the circuit in place to every matrix of `inputs` (qgd_Circuit.py:572);
+        inputs of one shape go through a single batched launch."""
+        if is_f32:
+            raise NotImplementedError("the GB300 engine computes in FP64 only")
+        params = self._params_dev(parameters_mtx)
+        groups = {}
+        for i, m in enumerate(inputs):
+            v = self._check_mtx(m)
+            groups.setdefault(v.shape, []).append(i)
+        for shape, idx in groups.items():
+            stack = dev.torch.from_numpy(np.stack([np.ascontiguousarray(self._check_mtx(inputs[i])) for i in idx]))
+            d = stack.cuda()
+            self.apply_to_device(params.reshape(1, -1).expand(len(idx), -1).contiguous(), d)
+            host = d.cpu().numpy()
+            for k, i in enumerate(idx):
+                self._check_mtx(inputs[i])[...] = host[k]
+
     def apply_from_right(self, parameters_mtx, unitary_mtx, parallel=1, is_f32=False):
         """In place ``unitary_mtx <- unitary_mtx C(parameters)`` (qgd_Circuit.py:559)."""
         if is_f32:

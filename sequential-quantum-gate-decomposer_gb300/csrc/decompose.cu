@@ -303,7 +303,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
   return f;
 }
 
-__global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
+__global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
   extern __shared__ double2 smem2[];
   const int b = blockIdx.x;
   if (b >= a.B) return;

@@ -125,6 +125,33 @@ class N_Qubit_Decomposition_custom:
     def get_Num_of_Iters(self):
         return self.num_iters
 
+    def get_Unitary(self):
+        """The matrix being decomposed (the U^dagger handed to the constructor)."""
+        return self.Umtx.copy()
+
+    def set_Unitary(self, Umtx):
+        U = np.asarray(Umtx)
+        if U.dtype != np.complex128 or U.shape != self.Umtx.shape:
+            raise ValueError("the new target must be complex128 with shape %s" % (self.Umtx.shape,))
+        self.Umtx = np.ascontiguousarray(U)
+        self._evaluator = None
+
+    def get_Gate_Num(self):
+        return self.circuit.get_Gate_Num()
+
+    def set_Iteration_Loops(self, iteration_loops):
+        """{qbit_num: loops} or an int: BFGS restarts per outer iteration (BFGS.cpp:67-99)."""
+        if isinstance(iteration_loops, dict):
+            loops = iteration_loops.get(self.qbit_num)
+            if loops is not None:
+                self.config["max_iteration_loops"] = int(loops)
+        else:
+            self.config["max_iteration_loops"] = int(iteration_loops)
+        return 0
+
+    def set_Convergence_Threshold(self, threshold):
+        self.config["convergence_threshold"] = float(threshold)
+
     # ---- cost / gradient -----------------------------------------------------------------
     def evaluator(self):
         if self._evaluator is None:

@@ -235,3 +235,47 @@ def test_errors_do_not_fall_back(sqg):
     c.add_U3(0)
     with pytest.raises(ValueError):
         c.get_Matrix(np.zeros(4))
+
+
+def test_engine_matches_golden_fixture_of_the_reference_target(sqg):
+    """Cost and adjoint gradient on the reference's own 4-qubit test target (golden fixture
+    from the oracle, tests/golden/make_golden.py), all three cost variants and a trace offset."""
+    import os
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "umtx4_golden.npz"))
+    c = sqg.Circuit(4)
+    for t, tg, ctl, ps in d["gates"]:
+        if t == 7:
+            c.add_U3(int(tg))
+        else:
+            c.add_CNOT(int(tg), int(ctl))
+    assert np.array_equal(c.gate_records(), d["gates"])
+    theta = torch.from_numpy(d["theta"]).cuda()
+    for name, v in (("frob", 0), ("hs", 3), ("infid", 9)):
+        cost, grad = sqg.CostEvaluator(c, d["target"], cost_variant=v).cost_grad(theta)
+        assert_close(cost.cpu().numpy(), d["cost_" + name])
+        assert_close(grad.cpu().numpy(), d["grad_" + name])
+    cost, grad = sqg.CostEvaluator(c, d["target_offset4"], trace_offset=4).cost_grad(theta)
+    assert_close(cost.cpu().numpy(), d["cost_offset4"])
+    assert_close(grad.cpu().numpy(), d["grad_offset4"])
+
+
+def test_apply_to_list_and_unitary_accessors(sqg):
+    n = 3
+    rng = np.random.default_rng(31)
+    c = spec_circuit(sqg, n, 15, rng)
+    p = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    ref = O.get_matrix(n, c.gate_records(), p)
+    mats = [rng.standard_normal((8, k)) + 1j * rng.standard_normal((8, k)) for k in (8, 3, 8, 1)]
+    orig = [m.copy() for m in mats]
+    c.apply_to_list(mats, p)
+    for m, o in zip(mats, orig):
+        assert_close(m, ref @ o)
+    U = O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, p.size))
+    d = sqg.N_Qubit_Decomposition_custom(U.conj().T)
+    assert np.array_equal(d.get_Unitary(), U.conj().T)
+    d.set_Unitary(np.eye(8, dtype=np.complex128))
+    d.set_Gate_Structure(c)
+    assert_close(d.Optimization_Problem(p), 1.0 - np.trace(ref).real / 8)
+    d.set_Iteration_Loops({3: 2})
+    assert d.config["max_iteration_loops"] == 2

@@ -220,3 +220,20 @@ def test_bfgs_decomposition_reaches_tolerance():
     assert np.all(costs < 1e-8)
     for b in range(2):
         assert O.cost(n, g, x[b], U.conj().T) < 1e-8
+
+
+def test_oracle_reproduces_golden_fixture_of_the_reference_target():
+    """tests/golden/umtx4_golden.npz holds the reference's own 4-qubit test target
+    (data/Umtx.mat) with costs and gradients; the oracle must keep reproducing them."""
+    import os
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "umtx4_golden.npz"))
+    g, th = d["gates"], d["theta"]
+    for name, v in (("frob", O.FROBENIUS_NORM), ("hs", O.HILBERT_SCHMIDT_TEST), ("infid", O.INFIDELITY)):
+        c, gr = O.batch(4, g, th, d["target"], variant=v, with_grad=True, nthreads=1)
+        assert np.array_equal(c, d["cost_" + name]) and np.array_equal(gr, d["grad_" + name])
+    c, gr = O.batch(4, g, th, d["target_offset4"], trace_offset=4, with_grad=True, nthreads=1)
+    assert np.array_equal(c, d["cost_offset4"]) and np.array_equal(gr, d["grad_offset4"])
+    # the stored target is unitary to the precision it was saved with (about 1e-8)
+    T = d["target"]
+    assert np.allclose(T @ T.conj().T, np.eye(16), atol=1e-7)
