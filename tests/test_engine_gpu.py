@@ -279,3 +279,25 @@ def test_apply_to_list_and_unitary_accessors(sqg):
     assert_close(d.Optimization_Problem(p), 1.0 - np.trace(ref).real / 8)
     d.set_Iteration_Loops({3: 2})
     assert d.config["max_iteration_loops"] == 2
+
+
+@pytest.mark.parametrize("kind", ["empty", "no_params"])
+def test_circuits_without_gates_or_parameters(sqg, kind):
+    """Edge cases of the reference's tests (test_circuit.py:1022-1041): an empty gate list and
+    a circuit of constant gates only."""
+    n = 3
+    c = sqg.Circuit(n)
+    if kind == "no_params":
+        c.add_CNOT(1, 0)
+        c.add_CZ(2, 1)
+    rng = np.random.default_rng(40)
+
+
+    target = np.ascontiguousarray((rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8))))
+    ev = sqg.CostEvaluator(c, target)
+    cost, grad = ev.cost_grad(torch.zeros((2, 0), dtype=torch.float64, device="cuda"))
+    rc = O.cost(n, c.gate_records(), np.zeros(0), target)
+    assert np.allclose(cost.cpu().numpy(), rc, atol=1e-14)
+    assert grad.shape == (2, 0)
+    assert np.allclose(c.get_Matrix(np.zeros(0)), O.get_matrix(n, c.gate_records(), np.zeros(0)), atol=1e-14)
+    assert c.apply_derivate_to(np.zeros(0), np.eye(8, dtype=np.complex128)) == []

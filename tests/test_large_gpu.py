@@ -82,3 +82,24 @@ def test_n12_fused_equals_unfused_and_stays_unitary(sqg, wl):
     ev = sqg.CostEvaluator(c, U.conj().T.contiguous())
     cost, _ = ev.cost_grad(th[0], with_grad=False)
     assert abs(cost.item()) < 1e-10
+
+
+def test_n13_maximum_size_cost_and_application(sqg, wl):
+    """The largest supported register: n = 13 (8192 x 8192 complex128, 1 GiB), cost only."""
+    rng = np.random.default_rng(24)
+    c = wl.random_gate_circuit(13, 40, rng)
+    p = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    N = 1 << 13
+    a = torch.eye(N, dtype=torch.complex128, device="cuda").reshape(1, N, N).contiguous()
+    th = torch.from_numpy(p).cuda().reshape(1, -1)
+    c.apply_to_device(th, a, fused=True)
+    b = torch.eye(N, dtype=torch.complex128, device="cuda").reshape(1, N, N).contiguous()
+    c.apply_to_device(th, b, fused=False)
+    torch.cuda.synchronize()
+    assert float((a - b).abs().max()) < 1e-12
+    del b
+    ev = sqg.CostEvaluator(c, a[0].conj().T.contiguous())
+    cost, _ = ev.cost_grad(th[0], with_grad=False)
+    assert abs(cost.item()) < 1e-10
+    with pytest.raises(Exception):
+        ev.cost_grad(th[0], with_grad=True)  # gradients are limited to 12 qubits
