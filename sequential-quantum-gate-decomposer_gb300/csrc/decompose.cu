@@ -27,6 +27,7 @@ using namespace sqg;
 namespace {
 
 constexpr int kDecThreads = 128;
+constexpr int kDecVectors = 16;  // P-vectors in shared memory (Sh::x ... Sh::zs)
 constexpr double kNumPrecision = 1.42e-14;  // grad_descend.cpp:37
 constexpr double kTwoPi = 6.283185307179586476925286766559;
 
@@ -45,6 +46,7 @@ struct DecArgs {
   unsigned long long seed;
   double* zglob;
   int z_in_smem;
+  int cyclic;  // cost and gradient through the environment matrix (dec_eval_cyclic)
 };
 
 struct Sh {
@@ -52,7 +54,7 @@ struct Sh {
   GateMat* gm;
   double* R;   // [L][8] reduced 2x2 overlaps of the reverse sweep
   int* pgate;  // gate owning each parameter
-  double *x, *g, *d, *x0, *g0, *gbest, *ztg, *delta, *gamma, *gtz, *nz, *bestx, *guess, *S;
+  double *x, *g, *d, *x0, *g0, *gbest, *ztg, *delta, *gamma, *gtz, *nz, *bestx, *guess, *S, *cs, *zs;
   double *Z, *redd, *tot, *scratch;
 };
 
@@ -70,34 +72,44 @@ __device__ double dot(const double* a, const double* b, int P, double* scratch) 
   return block_allsum(s, scratch);
 }
 
-// Cost and gradient of parameter vector xv (smem) for instance b; gradient into gv.
-__device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, double* gv, int b) {
-  const int N = a.N, cols = a.cols, off = a.trace_offset;
-  build_gate_mats(a.gates, a.L, xv, sh.gm, sh.sc);
-  const double2* T = a.targets + (long long)b * a.tstride;
-  for (int e = threadIdx.x; e < N * cols; e += blockDim.x) {
-    int r = e / cols, c = e - r * cols;
-    sh.psi[c * N + r] = T[e];
-    sh.lam[c * N + r] = make_double2(r == c + off ? 1.0 : 0.0, 0.0);
+// Gate matrices of parameter vector xv: one sincos per parameter (threads over
+// parameters, so every warp instruction of the FP64 series works on full warps), then the
+// 2x2 kernels from the stored (sin, cos) (threads over gates).  Same formulas as
+// build_gate_mats.
+__device__ void dec_build(const DecArgs& a, const Sh& sh, const double* xv) {
+  for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
+    double s, c;
+    sincos(xv[p], &s, &c);
+    sh.sc[p] = make_double2(s, c);
   }
   __syncthreads();
-  for (int g = 0; g < a.L; g++) {
-    Gate gt = a.gates[g];
-    tile_apply(sh.psi, N, a.n, cols, gt, make_op(gt.type, sh.gm[g], ORIENT_FWD));
-    __syncthreads();
+  for (int g = threadIdx.x; g < a.L; g += blockDim.x) {
+    const Gate gt = a.gates[g];
+    GateMat m;
+    m.u[0] = m.u[1] = m.u[2] = m.u[3] = make_double2(0.0, 0.0);
+    if (gt.type == G_U3) {
+      const double st = sh.sc[gt.pstart].x, ct = sh.sc[gt.pstart].y;
+      const double sp = sh.sc[gt.pstart + 1].x, cp = sh.sc[gt.pstart + 1].y;
+      const double sl = sh.sc[gt.pstart + 2].x, cl = sh.sc[gt.pstart + 2].y;
+      const double spl = sp * cl + cp * sl, cpl = cp * cl - sp * sl;
+      m.u[0] = make_double2(ct, 0.0);
+      m.u[1] = make_double2(-st * cl, -st * sl);
+      m.u[2] = make_double2(st * cp, st * sp);
+      m.u[3] = make_double2(ct * cpl, ct * spl);
+    } else if (gate_param_num(gt.type) == 1) {
+      m.u[0] = make_double2(sh.sc[gt.pstart].y, sh.sc[gt.pstart].x);
+    }
+    sh.gm[g] = m;
   }
-  double2 tr = tile_trace(sh.psi, N, cols, 0, off, sh.scratch);
-  double* Rb = sh.R;
-  // buffer each gate's overlap; the derivative contractions run afterwards for all
-  // parameters at once on full warps
-  adjoint_sweep(sh.psi, sh.lam, N, a.n, cols, a.gates, sh.gm, sh.sc, a.L, sh.redd, sh.tot,
-                [&](int g, const Gate&, const double* R) {
-                  if (threadIdx.x < 8) Rb[g * 8 + threadIdx.x] = R[threadIdx.x];
-                },
-                [](int) {});
-  __syncthreads();
+}
+
+// Cost of the variant from the trace tr and gradient from the buffered overlaps
+// sh.R (src-cpp/decomposition/Optimization_Interface.cpp:1395-1430 for the gradient
+// components, FROBENIUS_NORM with the reference's (1 - t/N) - 1 rounding).
+__device__ double dec_finish(const DecArgs& a, const Sh& sh, double2 tr, double* gv) {
+  const double* Rb = sh.R;
   double f;
-  const double dc = cols;
+  const double dc = a.cols;
   if (a.variant == SQG_FROBENIUS_NORM) {
     f = 1.0 - tr.x / dc;
   } else if (a.variant == SQG_HILBERT_SCHMIDT_TEST) {
@@ -125,7 +137,186 @@ __device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, dou
   return f;
 }
 
+// Barrier among the first aw warps of the CTA (the ones that run the sweep).
+__device__ __forceinline__ void sweep_sync(int aw) {
+  if (aw == (int)(blockDim.x >> 5))
+    __syncthreads();
+  else if (aw == 1)
+    __syncwarp();
+  else
+    asm volatile("bar.sync 1, %0;" ::"r"(aw * 32) : "memory");
+}
+
+// Overlap of gate gt from the environment matrix m (N x N, m[c * N + r] = M[r][c]):
+// R_ab = sum over the other qubits of M[(b, rest)][(a, rest)] (for a controlled gate only
+// the rest with the control bit set), written as R[2 * (2a + b) + {0, 1}].  Warp 0 only.
+__device__ __forceinline__ void cyclic_overlap(const double2* m, int n, int N, const Gate& gt, double* R) {
+  const int lane = threadIdx.x & 31;
+  const bool ctrl = gate_controlled(gt.type);
+  const int entries = 4 << (ctrl ? n - 2 : n - 1);
+  double2 v = make_double2(0.0, 0.0);
+  for (int j = lane; j < entries; j += 32) {
+    const int q = j & 3, ri = j >> 2;
+    const int rest = ctrl ? pair_index2(ri, gt.target, gt.control) : pair_index1(ri, gt.target);
+    const int row = rest | ((q & 1) << gt.target), col = rest | ((q >> 1) << gt.target);
+    const double2 e = m[col * N + row];
+    if (j == lane) {
+      v = e;
+    } else {
+      v.x += e.x;
+      v.y += e.y;
+    }
+  }
+  const int span = entries < 32 ? entries : 32;
+  for (int o = 4; o < span; o <<= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  if (lane < 4) {
+    R[2 * lane] = v.x;
+    R[2 * lane + 1] = v.y;
+  }
+}
+
+// Cost and adjoint gradient in the cyclic form, for targets with cols >= 3N/4 columns.
+// With psi_{k-1} = G_{k-1} ... G_0 T (the state in front of gate k) and lambda_k =
+// G_{k+1}^dagger ... G_{L-1}^dagger E (E: the columns e_{j + trace_offset}), the overlap
+// R_ab = sum conj(lambda_a) psi_b of gate k is a partial trace of the N x N matrix
+// M_k = psi_{k-1} lambda_k^dagger.  M_0 = T E^dagger G_{L-1} ... G_1 and
+// M_{k+1} = G_k M_k G_{k+1}^dagger, so one matrix carried through the circuit replaces the
+// state and adjoint sweeps and their per-gate inner products; tr(G_0 M_0) =
+// tr(E^dagger U T) is the trace of the cost.  M is a 2n-qubit register (row bits low,
+// column bits high): multiplying by G from the left applies G to qubit t, from the right
+// applies G^T (G^dagger: conj G) to qubit t + n.
+__device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* xv, double* gv, int b) {
+  const int n = a.n, N = a.N, NN = N * N, cols = a.cols, off = a.trace_offset, L = a.L;
+  dec_build(a, sh, xv);
+  double2* m = sh.psi;  // psi and lam are contiguous and hold >= N * N entries
+  const double2* T = a.targets + (long long)b * a.tstride;
+  for (int e = threadIdx.x; e < NN; e += blockDim.x) {
+    const int c = e >> n, r = e & (N - 1), j = c - off;
+    m[e] = (j >= 0 && j < cols) ? T[r * cols + j] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const int aw = min((int)(blockDim.x >> 5), (NN / 2 + 31) >> 5);
+  if ((int)(threadIdx.x >> 5) < aw) {
+    auto right = [&](int g, int orient) {
+      Gate gs = a.gates[g];
+      gs.target += n;
+      if (gate_controlled(gs.type)) gs.control += n;
+      tile_apply(m, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[g], orient));
+      sweep_sync(aw);
+    };
+    for (int g = L - 1; g >= 1; g--) right(g, ORIENT_TRANS);
+    for (int g = 0; g < L; g++) {
+      const Gate gt = a.gates[g];
+      if (gate_param_num(gt.type) > 0) {
+        if (threadIdx.x < 32) cyclic_overlap(m, n, N, gt, sh.R + g * 8);
+        sweep_sync(aw);
+      }
+      if (g == 0 || g < L - 1) {
+        tile_apply(m, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[g], ORIENT_FWD));
+        sweep_sync(aw);
+      }
+      if (g == 0 && threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double2 v = lane < N ? m[lane * N + lane] : make_double2(0.0, 0.0);
+        for (int o = 1; o < N; o <<= 1) {  // lanes 0..N-1 end with the full sum
+          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (lane == 0) {
+          sh.redd[0] = v.x;
+          sh.redd[1] = v.y;
+        }
+      }
+      if (g < L - 1) {
+        if (g == 0) sweep_sync(aw);
+        right(g + 1, ORIENT_CONJ);
+      }
+    }
+  }
+  __syncthreads();
+  const double2 tr = make_double2(sh.redd[0], sh.redd[1]);
+  return dec_finish(a, sh, tr, gv);
+}
+
+// Cost and gradient of parameter vector xv (smem) for instance b; gradient into gv.
+__device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, double* gv, int b) {
+  if (a.cyclic) return dec_eval_cyclic(a, sh, xv, gv, b);
+  const int N = a.N, cols = a.cols, off = a.trace_offset;
+  dec_build(a, sh, xv);
+  const double2* T = a.targets + (long long)b * a.tstride;
+  for (int e = threadIdx.x; e < N * cols; e += blockDim.x) {
+    int r = e / cols, c = e - r * cols;
+    sh.psi[c * N + r] = T[e];
+    sh.lam[c * N + r] = make_double2(r == c + off ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int g = 0; g < a.L; g++) {
+    Gate gt = a.gates[g];
+    tile_apply(sh.psi, N, a.n, cols, gt, make_op(gt.type, sh.gm[g], ORIENT_FWD));
+    __syncthreads();
+  }
+  double2 tr = tile_trace(sh.psi, N, cols, 0, off, sh.scratch);
+  double* Rb = sh.R;
+  // buffer each gate's overlap; the derivative contractions run afterwards for all
+  // parameters at once on full warps
+  adjoint_sweep(sh.psi, sh.lam, N, a.n, cols, a.gates, sh.gm, sh.sc, a.L, sh.redd, sh.tot,
+                [&](int g, const Gate&, const double* R) {
+                  if (threadIdx.x < 8) Rb[g * 8 + threadIdx.x] = R[threadIdx.x];
+                },
+                [](int) {});
+  __syncthreads();
+  return dec_finish(a, sh, tr, gv);
+}
+
+// out[k] = sum_{k <= i < P} a[i] b[i] for every k, in a fixed order (a suffix scan inside
+// each warp, then the totals of the later warps and of the later segments of blockDim
+// entries).  Called by all threads; ends with a barrier.
+__device__ void block_suffix_dot(double* out, const double* a, const double* b, int P, double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double carry = 0.0;
+  for (int seg = (P - 1) / (int)blockDim.x; seg >= 0; seg--) {
+    const int k = seg * blockDim.x + threadIdx.x;
+    double v = k < P ? a[k] * b[k] : 0.0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const double u = __shfl_down_sync(0xffffffffu, v, o);
+      if (lane + o < 32) v += u;
+    }
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    double later = carry;
+    for (int w = nw - 1; w > warp; w--) later += scratch[w];
+    if (k < P) out[k] = v + later;
+    if (seg > 0) {  // same order in every thread, so all threads carry the same value
+      double t = carry;
+      for (int w = nw - 1; w >= 0; w--) t += scratch[w];
+      carry = t;
+    }
+  }
+  __syncthreads();
+}
+
+// Maximum of an int over the CTA, returned to every thread.
+__device__ __forceinline__ int block_allmax_int(int v, double* scratch) {
+  int* s = reinterpret_cast<int*>(scratch);
+  v = __reduce_max_sync(0xffffffffu, v);
+  const int nw = blockDim.x >> 5;
+  if (nw == 1) return v;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int t = s[0];
+  for (int w = 1; w < nw; w++) t = max(t, s[w]);
+  return t;
+}
+
 // BFGS_Powell::BFGS_iteration (BFGS_Powell.cpp:202-396); returns the updated norm_Z.
+// Z is held as Zs diag(cs): the reference's final column scaling is recorded in cs and
+// folded into the next read of each column instead of a pass over Z.  sh.ztg = Z^T g0 and
+// sh.zs = cs * ztg come from the search direction of this iteration.
 __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z) {
   const int P = a.P;
   double* Z = sh.Z;
@@ -139,39 +330,43 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
   double dtg = dot(sh.gamma, sh.delta, P, sh.scratch);
   if (dtg < fabs(tmp) * 0.1) return norm_Z;
   dtg = fmax(kNumPrecision, dtg);
-  // Givens sweep from suffix sums of squares of ztg: the rotation at column col (pairing
-  // col-1 and col) has a = |ztg[col-1:]|, cv = ztg[col-1]/a, sv = r/a with r = |ztg[col:]|,
-  // or r = ztg[col] itself when everything after col is zero.
-  for (int k = threadIdx.x; k < P; k += blockDim.x) {
-    double s = 0.0;
-    for (int i = P - 1; i >= k; i--) s = fma(sh.ztg[i], sh.ztg[i], s);
-    sh.S[k] = s;
-  }
-  // last nonzero index of ztg
-  double lastnz = -1.0;
+  // The reference's Givens chain rotates z = ztg onto e_0 (columns col-1, col for
+  // col = m..1, m = last nonzero index).  With S_k = sum_{i>=k} z_i^2, r_k = sqrt(S_k) for
+  // k < m and r_m = z_m, the rotation at col has a = r_{col-1}, cos = z_{col-1} / a,
+  // sin = r_col / a, and the carry entering column col of a row y is
+  // sum_{i>=col} y_i z_i / r_col.  So the rotated row is
+  //   y'_col = alpha_col * sum_{i>=col} y_i z_i - beta_col * y_{col-1},
+  //   alpha_col = z_{col-1} / (r_{col-1} r_col),  beta_col = r_col / r_{col-1},
+  // three FP64 operations per entry instead of four, and no sequential hypot chain.
+  block_suffix_dot(sh.S, sh.ztg, sh.ztg, P, sh.scratch);
+  int lnz = -1;
   for (int i = threadIdx.x; i < P; i += blockDim.x)
-    if (sh.ztg[i] != 0.0) lastnz = fmax(lastnz, (double)i);
-  lastnz = -block_allmin(-lastnz, sh.scratch);
-  const int m = (int)lastnz;
-  __syncthreads();
-  for (int col = threadIdx.x + 1; col < P; col += blockDim.x) {
-    if (col <= m) {
-      double av = sqrt(sh.ztg[col - 1] * sh.ztg[col - 1] + sh.S[col]);
-      double r = col == m ? sh.ztg[col] : sqrt(sh.S[col]);
-      sh.gtz[col] = sh.ztg[col - 1] / av;  // cos
-      sh.nz[col] = r / av;                 // sin
-    }
+    if (sh.ztg[i] != 0.0) lnz = i;
+  const int m = block_allmax_int(lnz, sh.scratch);
+  for (int k = threadIdx.x; k <= m; k += blockDim.x) {
+    const double r = k == m ? sh.ztg[m] : sqrt(sh.S[k]);
+    sh.nz[k] = r;
+    sh.S[k] = 1.0 / r;
   }
   __syncthreads();
-  const int top = min(m, P - 1);
+  for (int col = threadIdx.x + 1; col <= m; col += blockDim.x) {
+    sh.gtz[col] = sh.ztg[col - 1] * sh.S[col - 1] * sh.S[col];   // alpha
+    sh.nz[col] = sh.nz[col] * sh.S[col - 1] * sh.cs[col - 1];       // beta, times the scale of column col-1
+  }
+  __syncthreads();
   for (int r = threadIdx.x; r < P; r += blockDim.x) {
     double* row = Z + (long long)r * P;
-    for (int col = top; col >= 1; col--) {
-      double cv = sh.gtz[col], sv = sh.nz[col];
-      double zc = row[col - 1], zn = row[col];
-      row[col] = cv * zn - sv * zc;
-      row[col - 1] = cv * zc + sv * zn;
+    if (m >= 1) {
+      double sd = 0.0, ycur = row[m];
+      for (int col = m; col >= 1; col--) {
+        const double yprev = row[col - 1];
+        sd = fma(ycur, sh.zs[col], sd);
+        row[col] = fma(sh.gtz[col], sd, -sh.nz[col] * yprev);
+        ycur = yprev;
+      }
     }
+    for (int c = max(m, 0) + 1; c < P; c++)
+      if (sh.cs[c] != 1.0) row[c] *= sh.cs[c];
   }
   if (norm_Z < 0.0) {
     norm_Z = norm_delta / dtg;
@@ -191,17 +386,18 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
     sh.gtz[c] = s / dtg;
   }
   __syncthreads();
-  for (int c = threadIdx.x + 1; c < P; c += blockDim.x) {
+  for (int c = threadIdx.x; c < P; c += blockDim.x) {
+    if (c == 0) {
+      sh.cs[0] = 1.0;
+      continue;
+    }
     double gc = sh.gtz[c], s = 0.0;
     for (int r = 0; r < P; r++) {
       double z = Z[(long long)r * P + c] - gc * sh.delta[r];
       Z[(long long)r * P + c] = z;
       s = fma(z, z, s);
     }
-    if (s < norm_Z && s > kNumPrecision) {
-      double sc = sqrt(norm_Z / s);
-      for (int r = 0; r < P; r++) Z[(long long)r * P + c] *= sc;
-    }
+    sh.cs[c] = (s < norm_Z && s > kNumPrecision) ? sqrt(norm_Z / s) : 1.0;
   }
   __syncthreads();
   return norm_Z;
@@ -212,22 +408,27 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
   const int P = a.P;
   double* Z = sh.Z;
   for (int i = threadIdx.x; i < P * P; i += blockDim.x) Z[i] = (i % (P + 1)) == 0 ? 1.0 : 0.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) sh.cs[i] = 1.0;
   double norm_Z = -1.0;
   double f = dec_eval(a, sh, sh.x, sh.g, b);
   calls++;
   if (a.early_stop && f < a.tol) return f;
   double fprev = fabs(f + f + 1.0);
   for (;;) {
+    // search direction d = -Z Z^T g with Z = Zs diag(cs) (get_search_direction,
+    // BFGS_Powell.cpp:407-446)
     for (int c = threadIdx.x; c < P; c += blockDim.x) {
       double s = 0.0;
       for (int r = 0; r < P; r++) s = fma(Z[(long long)r * P + c], sh.g[r], s);
-      sh.ztg[c] = s;
+      const double zt = s * sh.cs[c];
+      sh.ztg[c] = zt;
+      sh.zs[c] = zt * sh.cs[c];
     }
     __syncthreads();
     for (int r = threadIdx.x; r < P; r += blockDim.x) {
       const double* row = Z + (long long)r * P;
       double s = 0.0;
-      for (int c = 0; c < P; c++) s = fma(-row[c], sh.ztg[c], s);
+      for (int c = 0; c < P; c++) s = fma(-row[c], sh.zs[c], s);
       sh.d[r] = s;
     }
     __syncthreads();
@@ -303,7 +504,10 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
   return f;
 }
 
-__global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
+// At most 80 registers (6 CTAs of 128 threads per SM): the evaluation keeps only one warp
+// per CTA busy at n = 3, so resident CTAs are what hides FP64 and shared-memory latency
+// (measured 7470 vs 7103 decompositions/s with the unconstrained 126 registers).
+__global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   extern __shared__ double2 smem2[];
   const int b = blockIdx.x;
   if (b >= a.B) return;
@@ -318,7 +522,8 @@ __global__ void __launch_bounds__(kDecThreads) k_decompose(DecArgs a) {
   sh.R = (double*)take(sizeof(double) * 8 * max(L, 1));
   sh.pgate = (int*)take(sizeof(int) * max(P, 1));
   double** vecs[] = {&sh.x, &sh.g, &sh.d, &sh.x0, &sh.g0, &sh.gbest, &sh.ztg, &sh.delta, &sh.gamma,
-                     &sh.gtz, &sh.nz, &sh.bestx, &sh.guess, &sh.S};
+                     &sh.gtz, &sh.nz, &sh.bestx, &sh.guess, &sh.S, &sh.cs, &sh.zs};
+  static_assert(sizeof(vecs) / sizeof(vecs[0]) == kDecVectors, "dec_smem_bytes counts kDecVectors vectors");
   for (double** v : vecs) *v = (double*)take(sizeof(double) * max(P, 1));
   sh.redd = (double*)take(sizeof(double) * kTileMaxWarps * 8);
   sh.tot = (double*)take(sizeof(double) * 8);
@@ -373,7 +578,7 @@ size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem) {
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
   size_t s = 2 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
              r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) +
-             14 * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
+             kDecVectors * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
              r16(sizeof(double) * kTileMaxWarps);
   if (z_in_smem) s += r16(sizeof(double) * P * P);
   return s;
@@ -390,6 +595,17 @@ bool z_in_shared(const sqg_circuit* c, int cols) {
   if (zenv && std::string(zenv) == "global") return false;
   if (zenv && std::string(zenv) == "shared") return dec_smem_bytes(c, cols, true) <= 227 * 1024;
   return (size_t)c->P * c->P * sizeof(double) <= 16 * 1024 && dec_smem_bytes(c, cols, true) <= kDecSmemLimit;
+}
+
+// The environment-matrix form costs 3 N^2 / 2 amplitude-pair updates per gate against
+// 3 N cols / 2 for the state sweeps plus their per-gate inner products (the larger part
+// at full width); it wins from about cols >= 3N/4.  SQG_DECOMPOSE_FORM=sweep|cyclic
+// overrides the rule.
+bool use_cyclic(const sqg_circuit* c, int cols) {
+  const char* f = getenv("SQG_DECOMPOSE_FORM");
+  if (f && std::string(f) == "sweep") return false;
+  if (f && std::string(f) == "cyclic") return 2 * cols >= c->N;
+  return 4 * cols >= 3 * c->N;
 }
 
 }  // namespace
@@ -437,6 +653,7 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.seed = seed;
   a.zglob = (double*)workspace;
   a.z_in_smem = zs ? 1 : 0;
+  a.cyclic = use_cyclic(c, cols) ? 1 : 0;
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);

@@ -93,8 +93,9 @@ __device__ __forceinline__ void rule_rz(double2& x, double2& y, double c, double
   y = ny;
 }
 
-// Register copy of one gate's matrix, oriented for a forward (G), adjoint (G^dagger)
-// or transposed (G^T, used by right application) update.
+// Register copy of one gate's matrix, oriented for a forward (G), adjoint (G^dagger),
+// transposed (G^T: right multiplication by G) or conjugated (conj G = (G^dagger)^T: right
+// multiplication by G^dagger) update.
 struct PairOp {
   int kind;  // G_U3, G_RY (also CRY), G_RX, G_RZ, G_CNOT, G_CZ
   double a;  // u00 (U3) or cos
@@ -102,7 +103,7 @@ struct PairOp {
   double2 b, c, d;  // u01, u10, u11 (U3)
 };
 
-enum Orientation { ORIENT_FWD = 0, ORIENT_ADJ = 1, ORIENT_TRANS = 2 };
+enum Orientation { ORIENT_FWD = 0, ORIENT_ADJ = 1, ORIENT_TRANS = 2, ORIENT_CONJ = 3 };
 
 __device__ __forceinline__ PairOp make_op(int type, const GateMat& m, int orient) {
   PairOp op;
@@ -121,13 +122,17 @@ __device__ __forceinline__ PairOp make_op(int type, const GateMat& m, int orient
     } else if (orient == ORIENT_TRANS) {  // [[u00, u10], [u01, u11]]
       op.b = m.u[2];
       op.c = m.u[1];
+    } else if (orient == ORIENT_CONJ) {  // [[u00, conj u01], [conj u10, conj u11]]
+      op.b = make_double2(m.u[1].x, -m.u[1].y);
+      op.c = make_double2(m.u[2].x, -m.u[2].y);
+      op.d = make_double2(m.u[3].x, -m.u[3].y);
     }
   } else if (type == G_RY || type == G_CRY) {
-    // RY^dagger = RY^T = RY(-theta)
-    if (orient != ORIENT_FWD) op.s = -op.s;
+    // RY^dagger = RY^T = RY(-theta); RY is real, so conj RY = RY
+    if (orient == ORIENT_ADJ || orient == ORIENT_TRANS) op.s = -op.s;
   } else if (type == G_RX || type == G_RZ) {
-    // RX, RZ are symmetric: RX^T = RX, RZ^T = RZ; adjoint flips the sine.
-    if (orient == ORIENT_ADJ) op.s = -op.s;
+    // RX, RZ are symmetric: RX^T = RX, RZ^T = RZ; adjoint and conjugate flip the sine.
+    if (orient == ORIENT_ADJ || orient == ORIENT_CONJ) op.s = -op.s;
   }
   return op;
 }

@@ -16,22 +16,33 @@ def wl():
     return importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
 
 
-def test_first_bfgs_steps_follow_the_oracle(sqg, wl):
+@pytest.mark.parametrize("cols,offset,variant,form", [
+    (8, 0, O.FROBENIUS_NORM, None), (8, 0, O.FROBENIUS_NORM, "sweep"), (6, 2, O.FROBENIUS_NORM, None),
+    (4, 4, O.FROBENIUS_NORM, None), (4, 3, O.FROBENIUS_NORM, "cyclic"), (8, 0, O.HILBERT_SCHMIDT_TEST, None),
+    (8, 0, O.INFIDELITY, "sweep"), (8, 0, O.INFIDELITY, None)])
+def test_first_bfgs_steps_follow_the_oracle(sqg, wl, monkeypatch, cols, offset, variant, form):
     """With a small evaluation budget and no tolerance stop, the device BFGS lands where
-    the oracle's restatement of BFGS_Powell lands."""
+    the oracle's restatement of BFGS_Powell lands: square and rectangular targets with a
+    trace offset, all three cost variants, both forms of the device cost and gradient
+    (state sweeps, environment matrix)."""
+    if form:
+        monkeypatch.setenv("SQG_DECOMPOSE_FORM", form)
     n = 3
-    rng = np.random.default_rng(41)
+    rng = np.random.default_rng(41 + cols + offset + 10 * variant)
     c = wl.cnot_u3_ansatz(n, 5)
     P = c.get_Parameter_Num()
     recs = c.gate_records()
     B = 6
-    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, recs, rng.uniform(0, 2 * np.pi, P)).conj().T)
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, recs, rng.uniform(0, 2 * np.pi, P)).conj().T[:, offset:offset + cols])
                         for _ in range(B)])
     x0 = rng.uniform(0, 2 * np.pi, (B, P))
-    dec = sqg.BatchedDecomposer(c, tolerance=0.0, max_calls=6, max_outer=1, stop_at_tolerance=False)
+    dec = sqg.BatchedDecomposer(c, tolerance=0.0, max_calls=6, max_outer=1, stop_at_tolerance=False,
+                                trace_offset=offset, cost_variant=variant)
     x, cost, calls = dec.run(targets, x0)
     torch.cuda.synchronize()
-    xr, cr, callr = O.decompose(n, recs, targets, x0, tolerance=0.0, max_inner=6, max_outer=1)
+    off = offset if variant == O.FROBENIUS_NORM else 0
+    xr, cr, callr = O.decompose(n, recs, targets, x0, tolerance=0.0, max_inner=6, max_outer=1, trace_offset=off,
+                                variant=variant)
     assert np.array_equal(calls.cpu().numpy(), callr)
     assert np.allclose(cost.cpu().numpy(), cr, rtol=1e-9, atol=1e-12)
     assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)
