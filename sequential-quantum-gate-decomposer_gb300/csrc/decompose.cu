@@ -27,7 +27,7 @@ using namespace sqg;
 namespace {
 
 constexpr int kDecThreads = 128;
-constexpr int kDecVectors = 16;  // P-vectors in shared memory (Sh::x ... Sh::zs)
+constexpr int kDecVectors = 19;  // P-vectors in shared memory (Sh::x ... Sh::sdv)
 constexpr double kNumPrecision = 1.42e-14;  // grad_descend.cpp:37
 constexpr double kTwoPi = 6.283185307179586476925286766559;
 
@@ -54,7 +54,7 @@ struct Sh {
   GateMat* gm;
   double* R;   // [L][8] reduced 2x2 overlaps of the reverse sweep
   int* pgate;  // gate owning each parameter
-  double *x, *g, *d, *x0, *g0, *gbest, *ztg, *delta, *gamma, *gtz, *nz, *bestx, *guess, *S, *cs, *zs;
+  double *x, *g, *d, *x0, *g0, *gbest, *ztg, *delta, *gamma, *gtz, *nz, *bestx, *guess, *S, *cs, *zs, *v, *vp, *sdv;
   double *Z, *redd, *tot, *scratch;
 };
 
@@ -313,32 +313,79 @@ __device__ __forceinline__ int block_allmax_int(int v, double* scratch) {
   return t;
 }
 
+// Sums of K per-thread values over the CTA, returned to every thread in a fixed order.
+// scratch: K * kTileMaxWarps doubles.
+template <int K>
+__device__ __forceinline__ void block_allsum_n(double (&v)[K], double* scratch) {
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) scratch[k * kTileMaxWarps + warp] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double t = 0.0;
+    for (int w = 0; w < nw; w++) t += scratch[k * kTileMaxWarps + w];
+    v[k] = t;
+  }
+}
+
 // BFGS_Powell::BFGS_iteration (BFGS_Powell.cpp:202-396); returns the updated norm_Z.
-// Z is held as Zs diag(cs): the reference's final column scaling is recorded in cs and
-// folded into the next read of each column instead of a pass over Z.  sh.ztg = Z^T g0 and
-// sh.zs = cs * ztg come from the search direction of this iteration.
+//
+// Z is held as Zs diag(cs): column scalings are recorded in cs and folded into the next
+// read of the column.  On entry sh.ztg = Z^T g0 and sh.zs = cs * ztg (this iteration's
+// search direction); on exit they hold the same for the updated Z and the accepted
+// gradient g, so the next direction needs no Z^T g pass.
+//
+// Only one pass reads Z before the rotation: v = Z^T g.  With Q the reference's Givens
+// chain (Q^T ztg = |ztg| e_0), the reference's gTz = (Z Q)^T (g - g0) / dtg is, for the
+// columns c >= 1 it uses, (Q^T v)_c / dtg, and after the rank-one update and the scaling
+// by s_c, (Z_new^T g)_c = s_c ((Q^T v)_c - gTz_c (delta . g)); column 0 (delta / sqrt(dtg))
+// is dotted with g directly.
+//
+// The chain itself is evaluated in closed form: with S_k = sum_{i>=k} z_i^2, m the last
+// nonzero index of z = ztg, r_k = sqrt(S_k) (k < m) and r_m = z_m, the rotation at col
+// (pairing col-1, col; col = m..1) has a = r_{col-1}, cos = z_{col-1} / a, sin = r_col / a,
+// and the carry entering column col of a row y is sum_{i>=col} y_i z_i / r_col, so
+//   y'_col = alpha_col * sum_{i>=col} y_i z_i - beta_col * y_{col-1},
+//   alpha_col = z_{col-1} / (r_{col-1} r_col),  beta_col = r_col / r_{col-1}.
+// Keeping alpha_col as the column's new scale leaves two FP64 operations per entry.
 __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z) {
   const int P = a.P;
   double* Z = sh.Z;
+  double red[4] = {0.0, 0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
-    sh.delta[i] = sh.x[i] - sh.x0[i];
-    sh.gamma[i] = sh.g[i] - sh.g0[i];
+    const double de = sh.x[i] - sh.x0[i], ga = sh.g[i] - sh.g0[i];
+    sh.delta[i] = de;
+    sh.gamma[i] = ga;
+    red[0] = fma(de, de, red[0]);
+    red[1] = fma(sh.g0[i], de, red[1]);
+    red[2] = fma(ga, de, red[2]);
+    red[3] = fma(sh.g[i], de, red[3]);
   }
-  __syncthreads();
-  double norm_delta = dot(sh.delta, sh.delta, P, sh.scratch);
-  double tmp = dot(sh.g0, sh.delta, P, sh.scratch);
-  double dtg = dot(sh.gamma, sh.delta, P, sh.scratch);
-  if (dtg < fabs(tmp) * 0.1) return norm_Z;
+  for (int c = threadIdx.x; c < P; c += blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < P; r++) s = fma(Z[(long long)r * P + c], sh.g[r], s);
+    sh.v[c] = s * sh.cs[c];
+  }
+  block_allsum_n(red, sh.redd);
+  const double norm_delta = red[0], tmp = red[1], dgn = red[3];
+  double dtg = red[2];
+  if (dtg < fabs(tmp) * 0.1) {  // no update: Z^T g is v
+    for (int c = threadIdx.x; c < P; c += blockDim.x) {
+      sh.ztg[c] = sh.v[c];
+      sh.zs[c] = sh.v[c] * sh.cs[c];
+    }
+    __syncthreads();
+    return norm_Z;
+  }
   dtg = fmax(kNumPrecision, dtg);
-  // The reference's Givens chain rotates z = ztg onto e_0 (columns col-1, col for
-  // col = m..1, m = last nonzero index).  With S_k = sum_{i>=k} z_i^2, r_k = sqrt(S_k) for
-  // k < m and r_m = z_m, the rotation at col has a = r_{col-1}, cos = z_{col-1} / a,
-  // sin = r_col / a, and the carry entering column col of a row y is
-  // sum_{i>=col} y_i z_i / r_col.  So the rotated row is
-  //   y'_col = alpha_col * sum_{i>=col} y_i z_i - beta_col * y_{col-1},
-  //   alpha_col = z_{col-1} / (r_{col-1} r_col),  beta_col = r_col / r_{col-1},
-  // three FP64 operations per entry instead of four, and no sequential hypot chain.
   block_suffix_dot(sh.S, sh.ztg, sh.ztg, P, sh.scratch);
+  block_suffix_dot(sh.sdv, sh.v, sh.ztg, P, sh.scratch);
   int lnz = -1;
   for (int i = threadIdx.x; i < P; i += blockDim.x)
     if (sh.ztg[i] != 0.0) lnz = i;
@@ -349,24 +396,46 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
     sh.S[k] = 1.0 / r;
   }
   __syncthreads();
-  for (int col = threadIdx.x + 1; col <= m; col += blockDim.x) {
-    sh.gtz[col] = sh.ztg[col - 1] * sh.S[col - 1] * sh.S[col];   // alpha
-    sh.nz[col] = sh.nz[col] * sh.S[col - 1] * sh.cs[col - 1];       // beta, times the scale of column col-1
+  // per column: Q^T v (vp), the new scale alpha (nz), q = -beta cs_{col-1} / alpha (gtz)
+  // and beta cs_{col-1} (sdv) for the three-operation form used when some alpha is 0
+  bool zero_alpha = false;
+  for (int col = threadIdx.x; col < P; col += blockDim.x) {
+    if (col == 0) continue;
+    if (col > m) {
+      sh.vp[col] = sh.v[col];
+      continue;
+    }
+    const double ir0 = sh.S[col - 1], ir1 = sh.S[col], zc = sh.ztg[col - 1];
+    const double al = zc * ir0 * ir1, be = sh.nz[col] * ir0;
+    sh.vp[col] = fma(al, sh.sdv[col], -be * sh.v[col - 1]);
+    const double bc = be * sh.cs[col - 1];
+    sh.sdv[col] = bc;
+    sh.nz[col] = al;
+    if (zc != 0.0)
+      sh.gtz[col] = -bc / al;
+    else
+      zero_alpha = true;
   }
-  __syncthreads();
+  zero_alpha = __syncthreads_or(zero_alpha);
   for (int r = threadIdx.x; r < P; r += blockDim.x) {
     double* row = Z + (long long)r * P;
-    if (m >= 1) {
-      double sd = 0.0, ycur = row[m];
+    if (m < 1) break;
+    double sd = 0.0, ycur = row[m];
+    if (!zero_alpha) {
       for (int col = m; col >= 1; col--) {
         const double yprev = row[col - 1];
         sd = fma(ycur, sh.zs[col], sd);
-        row[col] = fma(sh.gtz[col], sd, -sh.nz[col] * yprev);
+        row[col] = fma(sh.gtz[col], yprev, sd);  // times alpha_col (the column's scale)
+        ycur = yprev;
+      }
+    } else {
+      for (int col = m; col >= 1; col--) {
+        const double yprev = row[col - 1];
+        sd = fma(ycur, sh.zs[col], sd);
+        row[col] = fma(sh.nz[col], sd, -sh.sdv[col] * yprev);
         ycur = yprev;
       }
     }
-    for (int c = max(m, 0) + 1; c < P; c++)
-      if (sh.cs[c] != 1.0) row[c] *= sh.cs[c];
   }
   if (norm_Z < 0.0) {
     norm_Z = norm_delta / dtg;
@@ -375,56 +444,67 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
     norm_Z = fmin(norm_Z, t);
     norm_Z = fmax(norm_Z, t * 0.1);
   }
-  const double sd = sqrt(dtg);
+  const double sdt = sqrt(dtg);
   __syncthreads();
-  for (int r = threadIdx.x; r < P; r += blockDim.x)
-    Z[(long long)r * P] = fabs(sh.delta[r]) > kNumPrecision ? sh.delta[r] / sd : 0.0;
-  __syncthreads();
-  for (int c = threadIdx.x + 1; c < P; c += blockDim.x) {
-    double s = 0.0;
-    for (int r = 0; r < P; r++) s = fma(sh.gamma[r], Z[(long long)r * P + c], s);
-    sh.gtz[c] = s / dtg;
+  double c0 = 0.0;
+  for (int r = threadIdx.x; r < P; r += blockDim.x) {
+    const double z0 = fabs(sh.delta[r]) > kNumPrecision ? sh.delta[r] / sdt : 0.0;
+    Z[(long long)r * P] = z0;
+    c0 = fma(z0, sh.g[r], c0);
   }
+  for (int col = threadIdx.x + 1; col <= m; col += blockDim.x) sh.cs[col] = zero_alpha ? 1.0 : sh.nz[col];
+  c0 = block_allsum(c0, sh.scratch);
   __syncthreads();
   for (int c = threadIdx.x; c < P; c += blockDim.x) {
     if (c == 0) {
       sh.cs[0] = 1.0;
+      sh.ztg[0] = c0;
+      sh.zs[0] = c0;
       continue;
     }
-    double gc = sh.gtz[c], s = 0.0;
+    const double cs = sh.cs[c], gtz = sh.vp[c] / dtg, gc = gtz / cs;
+    double s = 0.0;
     for (int r = 0; r < P; r++) {
       double z = Z[(long long)r * P + c] - gc * sh.delta[r];
       Z[(long long)r * P + c] = z;
       s = fma(z, z, s);
     }
-    sh.cs[c] = (s < norm_Z && s > kNumPrecision) ? sqrt(norm_Z / s) : 1.0;
+    const double nzc = s * cs * cs;
+    const double sc = (nzc < norm_Z && nzc > kNumPrecision) ? sqrt(norm_Z / nzc) : 1.0;
+    const double zt = sc * fma(-gtz, dgn, sh.vp[c]);
+    sh.cs[c] = cs * sc;
+    sh.ztg[c] = zt;
+    sh.zs[c] = zt * (cs * sc);
   }
   __syncthreads();
   return norm_Z;
 }
 
-// BFGS_Powell::Optimize from sh.x (updated in place).  Returns the final cost.
+// BFGS_Powell::Optimize from sh.x (updated in place).  Returns the final cost.  The
+// evaluation budget a.max_calls applies to this run (a new BFGS_Powell with its own call
+// count per restart, optimization_engines/BFGS.cpp:121-125); calls and iters accumulate
+// over the runs of the decomposition.
 __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, int& iters) {
+  int run = 0;
   const int P = a.P;
   double* Z = sh.Z;
   for (int i = threadIdx.x; i < P * P; i += blockDim.x) Z[i] = (i % (P + 1)) == 0 ? 1.0 : 0.0;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) sh.cs[i] = 1.0;
   double norm_Z = -1.0;
   double f = dec_eval(a, sh, sh.x, sh.g, b);
   calls++;
+  run++;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    sh.cs[i] = 1.0;
+    sh.ztg[i] = sh.g[i];
+    sh.zs[i] = sh.g[i];
+  }
+  __syncthreads();
   if (a.early_stop && f < a.tol) return f;
   double fprev = fabs(f + f + 1.0);
   for (;;) {
     // search direction d = -Z Z^T g with Z = Zs diag(cs) (get_search_direction,
-    // BFGS_Powell.cpp:407-446)
-    for (int c = threadIdx.x; c < P; c += blockDim.x) {
-      double s = 0.0;
-      for (int r = 0; r < P; r++) s = fma(Z[(long long)r * P + c], sh.g[r], s);
-      const double zt = s * sh.cs[c];
-      sh.ztg[c] = zt;
-      sh.zs[c] = zt * sh.cs[c];
-    }
-    __syncthreads();
+    // BFGS_Powell.cpp:407-446); Z^T g (sh.ztg) and cs * Z^T g (sh.zs) come from the last
+    // update or, for Z = I, are g itself
     for (int r = threadIdx.x; r < P; r += blockDim.x) {
       const double* row = Z + (long long)r * P;
       double s = 0.0;
@@ -444,7 +524,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
     double gn = dot(sh.g, sh.g, P, sh.scratch);
     if (gn <= 1e-19 * 1e-19 || dg >= 0.0 || f >= fprev) break;
     fprev = f;
-    if (calls >= a.max_calls) break;
+    if (run >= a.max_calls) break;
     iters++;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
       sh.x0[i] = sh.x[i];
@@ -460,6 +540,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
       __syncthreads();
       f = dec_eval(a, sh, sh.x, sh.g, b);
       calls++;
+      run++;
       if (a.early_stop && f < a.tol) return f;
       double dgc = dot(sh.d, sh.g, P, sh.scratch);
       if (f < f_best || fabs(dgc) < dg_best) {
@@ -469,7 +550,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
         for (int i = threadIdx.x; i < P; i += blockDim.x) sh.gbest[i] = sh.g[i];
         __syncthreads();
       }
-      if (calls == a.max_calls) break;
+      if (run == a.max_calls) break;
       if (f < f_low + step * 0.1 * dg) {
         if (dgc >= dg * 0.7) break;
         s_low = step;
@@ -522,7 +603,7 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   sh.R = (double*)take(sizeof(double) * 8 * max(L, 1));
   sh.pgate = (int*)take(sizeof(int) * max(P, 1));
   double** vecs[] = {&sh.x, &sh.g, &sh.d, &sh.x0, &sh.g0, &sh.gbest, &sh.ztg, &sh.delta, &sh.gamma,
-                     &sh.gtz, &sh.nz, &sh.bestx, &sh.guess, &sh.S, &sh.cs, &sh.zs};
+                     &sh.gtz, &sh.nz, &sh.bestx, &sh.guess, &sh.S, &sh.cs, &sh.zs, &sh.v, &sh.vp, &sh.sdv};
   static_assert(sizeof(vecs) / sizeof(vecs[0]) == kDecVectors, "dec_smem_bytes counts kDecVectors vectors");
   for (double** v : vecs) *v = (double*)take(sizeof(double) * max(P, 1));
   sh.redd = (double*)take(sizeof(double) * kTileMaxWarps * 8);

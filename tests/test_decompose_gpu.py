@@ -94,3 +94,24 @@ def test_rejects_unsupported(sqg, wl):
     c = wl.cnot_u3_ansatz(6, 2)
     with pytest.raises(Exception):
         sqg.BatchedDecomposer(c).run(np.zeros((1, 64, 64), dtype=np.complex128), np.zeros((1, c.get_Parameter_Num())))
+
+
+def test_every_restart_gets_its_own_budget(sqg, wl):
+    """The evaluation limit bounds each BFGS run, not the whole decomposition: a fresh
+    BFGS_Powell (with its own call count) per restart, optimization_engines/BFGS.cpp:121-125."""
+    n = 3
+    rng = np.random.default_rng(70)
+    c = wl.cnot_u3_ansatz(n, 2)  # cannot represent a Haar-random 3-qubit unitary
+    P = c.get_Parameter_Num()
+    B = 16
+    targets = np.stack([np.ascontiguousarray(wl.haar_unitary(8, rng).conj().T) for _ in range(B)])
+    x0 = rng.uniform(0, 2 * np.pi, (B, P))
+    max_calls, outer = 12, 3
+    _, cost, calls = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=max_calls, max_outer=outer).run(targets, x0)
+    torch.cuda.synchronize()
+    calls = calls.cpu().numpy()
+    assert np.all(cost.cpu().numpy() > 1e-8)
+    assert np.all(calls <= outer * max_calls)
+    assert np.all(calls > max_calls)  # the restarts ran
+    _, _, callr = O.decompose(n, c.gate_records(), targets, x0, tolerance=1e-8, max_inner=max_calls, max_outer=outer)
+    assert np.all(callr > max_calls) and np.all(callr <= outer * max_calls)
