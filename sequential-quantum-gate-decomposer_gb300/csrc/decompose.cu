@@ -27,6 +27,7 @@ using namespace sqg;
 namespace {
 
 constexpr int kDecThreads = 128;
+constexpr int kChunk = 8;        // Z entries per load batch in the row and column passes
 constexpr int kDecVectors = 19;  // P-vectors in shared memory (Sh::x ... Sh::sdv)
 constexpr double kNumPrecision = 1.42e-14;  // grad_descend.cpp:37
 constexpr double kTwoPi = 6.283185307179586476925286766559;
@@ -47,9 +48,13 @@ struct DecArgs {
   double* zglob;
   int z_in_smem;
   int cyclic;  // cost and gradient through the environment matrix (dec_eval_cyclic)
+  int chains;  // 2: the two-warp form dec_eval_cyclic2, split at gate `split`
+  int split;
 };
 
 struct Sh {
+  const Gate* gates;    // shared-memory copy of the gate list
+  const double2* tgt;  // shared-memory copy of this instance's target (N x cols, row-major)
   double2 *psi, *lam, *sc;
   GateMat* gm;
   double* R;   // [L][8] reduced 2x2 overlaps of the reverse sweep
@@ -84,7 +89,7 @@ __device__ void dec_build(const DecArgs& a, const Sh& sh, const double* xv) {
   }
   __syncthreads();
   for (int g = threadIdx.x; g < a.L; g += blockDim.x) {
-    const Gate gt = a.gates[g];
+    const Gate gt = sh.gates[g];
     GateMat m;
     m.u[0] = m.u[1] = m.u[2] = m.u[3] = make_double2(0.0, 0.0);
     if (gt.type == G_U3) {
@@ -120,7 +125,7 @@ __device__ double dec_finish(const DecArgs& a, const Sh& sh, double2 tr, double*
   }
   for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
     const int g = sh.pgate[p];
-    const Gate gt = a.gates[g];
+    const Gate gt = sh.gates[g];
     double2 t = contract_derivative(gt, sh.sc, p - gt.pstart, Rb + g * 8);
     double gvv;
     if (a.variant == SQG_FROBENIUS_NORM) {
@@ -192,7 +197,7 @@ __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* 
   const int n = a.n, N = a.N, NN = N * N, cols = a.cols, off = a.trace_offset, L = a.L;
   dec_build(a, sh, xv);
   double2* m = sh.psi;  // psi and lam are contiguous and hold >= N * N entries
-  const double2* T = a.targets + (long long)b * a.tstride;
+  const double2* T = sh.tgt;
   for (int e = threadIdx.x; e < NN; e += blockDim.x) {
     const int c = e >> n, r = e & (N - 1), j = c - off;
     m[e] = (j >= 0 && j < cols) ? T[r * cols + j] : make_double2(0.0, 0.0);
@@ -201,7 +206,7 @@ __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* 
   const int aw = min((int)(blockDim.x >> 5), (NN / 2 + 31) >> 5);
   if ((int)(threadIdx.x >> 5) < aw) {
     auto right = [&](int g, int orient) {
-      Gate gs = a.gates[g];
+      Gate gs = sh.gates[g];
       gs.target += n;
       if (gate_controlled(gs.type)) gs.control += n;
       tile_apply(m, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[g], orient));
@@ -209,7 +214,7 @@ __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* 
     };
     for (int g = L - 1; g >= 1; g--) right(g, ORIENT_TRANS);
     for (int g = 0; g < L; g++) {
-      const Gate gt = a.gates[g];
+      const Gate gt = sh.gates[g];
       if (gate_param_num(gt.type) > 0) {
         if (threadIdx.x < 32) cyclic_overlap(m, n, N, gt, sh.R + g * 8);
         sweep_sync(aw);
@@ -241,12 +246,119 @@ __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* 
   return dec_finish(a, sh, tr, gv);
 }
 
+// Two-warp form of dec_eval_cyclic for square targets (cols = N, no trace offset) with
+// N^2 / 2 <= 32 amplitude pairs, so that one warp holds one environment matrix.  Warp 0
+// builds psi_{h-1} = G_{h-1} ... G_0 T and warp 1 W = lambda_h^dagger = G_{L-1} ... G_{h+1}
+// (right products on the identity) at the same time; M_h = psi_{h-1} W is one N x N
+// product shared by both warps; then warp 1 runs M_{k+1} = G_k M_k G_{k+1}^dagger up to
+// gate L-1 (taking tr(G_h M_h) on the way) and warp 0 runs M_k = G_k^dagger M_{k+1}
+// G_{k+1} down to gate 0, each taking the overlaps of its own gates.  The FP64 work is that
+// of the one-warp form plus the product; the latency of an evaluation is about halved,
+// which is what a CTA running alone (the end of a batch, small batches) waits for.
+__device__ double dec_eval_cyclic2(const DecArgs& a, const Sh& sh, const double* xv, double* gv) {
+  const int n = a.n, N = a.N, NN = N * N, L = a.L, h = a.split;
+  dec_build(a, sh, xv);
+  __syncthreads();
+  double2* mA = sh.psi;
+  double2* mB = sh.lam;  // cols = N: each region holds N * N entries
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto shifted = [&](int g) {
+    Gate gs = sh.gates[g];
+    gs.target += n;
+    if (gate_controlled(gs.type)) gs.control += n;
+    return gs;
+  };
+  if (warp == 0) {
+    for (int e = lane; e < NN; e += 32) mA[e] = sh.tgt[(e & (N - 1)) * N + (e >> n)];
+    __syncwarp();
+    for (int k = 0; k < h; k++) {
+      const Gate gt = sh.gates[k];
+      tile_apply_by(mA, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[k], ORIENT_FWD), lane, 32);
+      __syncwarp();
+    }
+  } else if (warp == 1) {
+    for (int e = lane; e < NN; e += 32) mB[e] = make_double2((e & (N - 1)) == (e >> n) ? 1.0 : 0.0, 0.0);
+    __syncwarp();
+    for (int k = L - 1; k > h; k--) {
+      const Gate gs = shifted(k);
+      tile_apply_by(mB, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[k], ORIENT_TRANS), lane, 32);
+      __syncwarp();
+    }
+  }
+  if (warp < 2) {
+    // M_h[y][x] = sum_c psi[y][c] W[c][x], entry x * N + y, one per thread of the two warps
+    asm volatile("bar.sync 2, 64;" ::: "memory");
+    const int e = threadIdx.x;
+    double2 acc = make_double2(0.0, 0.0);
+    if (e < NN) {
+      const int x = e >> n, y = e & (N - 1);
+      for (int c = 0; c < N; c++) {
+        const double2 p = mA[c * N + y], w = mB[x * N + c];
+        acc.x = fma(p.x, w.x, fma(-p.y, w.y, acc.x));
+        acc.y = fma(p.x, w.y, fma(p.y, w.x, acc.y));
+      }
+    }
+    asm volatile("bar.sync 2, 64;" ::: "memory");
+    if (e < NN) {
+      mA[e] = acc;
+      mB[e] = acc;
+    }
+    asm volatile("bar.sync 2, 64;" ::: "memory");
+  }
+  if (warp == 1) {
+    for (int k = h; k < L; k++) {
+      const Gate gt = sh.gates[k];
+      if (gate_param_num(gt.type) > 0) {
+        cyclic_overlap(mB, n, N, gt, sh.R + k * 8);
+        __syncwarp();
+      }
+      if (k == h || k < L - 1) {
+        tile_apply_by(mB, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[k], ORIENT_FWD), lane, 32);
+        __syncwarp();
+      }
+      if (k == h) {  // tr(G_h M_h) = tr(E^dagger U T)
+        double2 v = lane < N ? mB[lane * N + lane] : make_double2(0.0, 0.0);
+        for (int o = 1; o < N; o <<= 1) {
+          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (lane == 0) {
+          sh.redd[0] = v.x;
+          sh.redd[1] = v.y;
+        }
+        __syncwarp();
+      }
+      if (k < L - 1) {
+        const Gate gs = shifted(k + 1);
+        tile_apply_by(mB, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[k + 1], ORIENT_CONJ), lane, 32);
+        __syncwarp();
+      }
+    }
+  } else if (warp == 0) {
+    for (int k = h - 1; k >= 0; k--) {
+      const Gate gt = sh.gates[k];
+      tile_apply_by(mA, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[k], ORIENT_ADJ), lane, 32);
+      __syncwarp();
+      const Gate gs = shifted(k + 1);
+      tile_apply_by(mA, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[k + 1], ORIENT_TRANS), lane, 32);
+      __syncwarp();
+      if (gate_param_num(gt.type) > 0) {
+        cyclic_overlap(mA, n, N, gt, sh.R + k * 8);
+        __syncwarp();
+      }
+    }
+  }
+  __syncthreads();
+  return dec_finish(a, sh, make_double2(sh.redd[0], sh.redd[1]), gv);
+}
+
 // Cost and gradient of parameter vector xv (smem) for instance b; gradient into gv.
 __device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, double* gv, int b) {
+  if (a.chains == 2) return dec_eval_cyclic2(a, sh, xv, gv);
   if (a.cyclic) return dec_eval_cyclic(a, sh, xv, gv, b);
   const int N = a.N, cols = a.cols, off = a.trace_offset;
   dec_build(a, sh, xv);
-  const double2* T = a.targets + (long long)b * a.tstride;
+  const double2* T = sh.tgt;
   for (int e = threadIdx.x; e < N * cols; e += blockDim.x) {
     int r = e / cols, c = e - r * cols;
     sh.psi[c * N + r] = T[e];
@@ -254,7 +366,7 @@ __device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, dou
   }
   __syncthreads();
   for (int g = 0; g < a.L; g++) {
-    Gate gt = a.gates[g];
+    Gate gt = sh.gates[g];
     tile_apply(sh.psi, N, a.n, cols, gt, make_op(gt.type, sh.gm[g], ORIENT_FWD));
     __syncthreads();
   }
@@ -262,7 +374,7 @@ __device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, dou
   double* Rb = sh.R;
   // buffer each gate's overlap; the derivative contractions run afterwards for all
   // parameters at once on full warps
-  adjoint_sweep(sh.psi, sh.lam, N, a.n, cols, a.gates, sh.gm, sh.sc, a.L, sh.redd, sh.tot,
+  adjoint_sweep(sh.psi, sh.lam, N, a.n, cols, sh.gates, sh.gm, sh.sc, a.L, sh.redd, sh.tot,
                 [&](int g, const Gate&, const double* R) {
                   if (threadIdx.x < 8) Rb[g * 8 + threadIdx.x] = R[threadIdx.x];
                 },
@@ -369,6 +481,7 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
   }
   for (int c = threadIdx.x; c < P; c += blockDim.x) {
     double s = 0.0;
+#pragma unroll 8
     for (int r = 0; r < P; r++) s = fma(Z[(long long)r * P + c], sh.g[r], s);
     sh.v[c] = s * sh.cs[c];
   }
@@ -417,24 +530,37 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
       zero_alpha = true;
   }
   zero_alpha = __syncthreads_or(zero_alpha);
+  // Rows in chunks of kChunk columns: all loads of a chunk are issued before its stores,
+  // so a row costs one memory round trip per chunk instead of one per column (a lone
+  // CTA, as at the end of a batch, sees the full L2 latency).
   for (int r = threadIdx.x; r < P; r += blockDim.x) {
     double* row = Z + (long long)r * P;
     if (m < 1) break;
     double sd = 0.0, ycur = row[m];
-    if (!zero_alpha) {
-      for (int col = m; col >= 1; col--) {
-        const double yprev = row[col - 1];
-        sd = fma(ycur, sh.zs[col], sd);
-        row[col] = fma(sh.gtz[col], yprev, sd);  // times alpha_col (the column's scale)
-        ycur = yprev;
+    for (int col = m; col >= 1; col -= kChunk) {
+      double yp[kChunk], out[kChunk];
+#pragma unroll
+      for (int j = 0; j < kChunk; j++) yp[j] = col - 1 - j >= 0 ? row[col - 1 - j] : 0.0;
+      if (!zero_alpha) {
+#pragma unroll
+        for (int j = 0; j < kChunk; j++) {
+          const int cc = max(col - j, 1);
+          sd = fma(ycur, sh.zs[cc], sd);
+          out[j] = fma(sh.gtz[cc], yp[j], sd);  // times alpha_cc (the column's scale)
+          ycur = yp[j];
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < kChunk; j++) {
+          const int cc = max(col - j, 1);
+          sd = fma(ycur, sh.zs[cc], sd);
+          out[j] = fma(sh.nz[cc], sd, -sh.sdv[cc] * yp[j]);
+          ycur = yp[j];
+        }
       }
-    } else {
-      for (int col = m; col >= 1; col--) {
-        const double yprev = row[col - 1];
-        sd = fma(ycur, sh.zs[col], sd);
-        row[col] = fma(sh.nz[col], sd, -sh.sdv[col] * yprev);
-        ycur = yprev;
-      }
+#pragma unroll
+      for (int j = 0; j < kChunk; j++)
+        if (col - j >= 1) row[col - j] = out[j];
     }
   }
   if (norm_Z < 0.0) {
@@ -464,10 +590,20 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
     }
     const double cs = sh.cs[c], gtz = sh.vp[c] / dtg, gc = gtz / cs;
     double s = 0.0;
-    for (int r = 0; r < P; r++) {
-      double z = Z[(long long)r * P + c] - gc * sh.delta[r];
-      Z[(long long)r * P + c] = z;
-      s = fma(z, z, s);
+    for (int r0 = 0; r0 < P; r0 += kChunk) {
+      double zv[kChunk];
+#pragma unroll
+      for (int j = 0; j < kChunk; j++) zv[j] = r0 + j < P ? Z[(long long)(r0 + j) * P + c] : 0.0;
+#pragma unroll
+      for (int j = 0; j < kChunk; j++) {
+        if (r0 + j < P) {
+          zv[j] = zv[j] - gc * sh.delta[r0 + j];
+          s = fma(zv[j], zv[j], s);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kChunk; j++)
+        if (r0 + j < P) Z[(long long)(r0 + j) * P + c] = zv[j];
     }
     const double nzc = s * cs * cs;
     const double sc = (nzc < norm_Z && nzc > kNumPrecision) ? sqrt(norm_Z / nzc) : 1.0;
@@ -508,6 +644,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
     for (int r = threadIdx.x; r < P; r += blockDim.x) {
       const double* row = Z + (long long)r * P;
       double s = 0.0;
+#pragma unroll 8
       for (int c = 0; c < P; c++) s = fma(-row[c], sh.zs[c], s);
       sh.d[r] = s;
     }
@@ -596,6 +733,10 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   Sh sh;
   char* p = reinterpret_cast<char*>(smem2);
   auto take = [&](size_t bytes) { char* r = p; p += (bytes + 15) / 16 * 16; return r; };
+  Gate* gsh = (Gate*)take(sizeof(Gate) * max(L, 1));
+  sh.gates = gsh;
+  double2* tsh = (double2*)take(sizeof(double2) * NC);
+  sh.tgt = tsh;
   sh.psi = (double2*)take(sizeof(double2) * NC);
   sh.lam = (double2*)take(sizeof(double2) * NC);
   sh.gm = (GateMat*)take(sizeof(GateMat) * max(L, 1));
@@ -611,8 +752,10 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   sh.scratch = (double*)take(sizeof(double) * kTileMaxWarps);
   sh.Z = a.z_in_smem ? (double*)take(sizeof(double) * P * P) : a.zglob + (long long)b * P * P;
 
+  for (int e = threadIdx.x; e < NC; e += blockDim.x) tsh[e] = a.targets[(long long)b * a.tstride + e];
   for (int g = threadIdx.x; g < L; g += blockDim.x) {
     Gate gt = a.gates[g];
+    gsh[g] = gt;
     for (int k = 0; k < gate_param_num(gt.type); k++) sh.pgate[gt.pstart + k] = g;
   }
   for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = a.x[(long long)b * P + i];
@@ -657,7 +800,7 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
 size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem) {
   auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
-  size_t s = 2 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
+  size_t s = r16(sizeof(Gate) * L) + 3 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
              r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) +
              kDecVectors * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
              r16(sizeof(double) * kTileMaxWarps);
@@ -687,6 +830,39 @@ bool use_cyclic(const sqg_circuit* c, int cols) {
   if (f && std::string(f) == "sweep") return false;
   if (f && std::string(f) == "cyclic") return 2 * cols >= c->N;
   return 4 * cols >= 3 * c->N;
+}
+
+bool use_two_chains() {
+  const char* f = getenv("SQG_DECOMPOSE_CHAINS");
+  return !(f && std::string(f) == "1");
+}
+
+// Split gate h of the two-warp evaluation: minimises max(phase 1) + max(phase 2) of the
+// two warps with the FP64 cost of each gate application (U3 14, one-parameter 8, CNOT/CZ
+// about 1 for the exchange).
+int two_chain_split(const sqg_circuit& c) {
+  const int L = c.L;
+  std::vector<double> w(L);
+  for (int k = 0; k < L; k++) {
+    const int t = c.h_gates[k].type;
+    w[k] = t == G_U3 ? 14.0 : gate_param_num(t) == 1 ? 8.0 : 1.0;
+  }
+  int best = 1;
+  double best_t = 1e300;
+  for (int h = 1; h < L; h++) {
+    double p1a = 0, p1b = 0, p2a = 0, p2b = 0;
+    for (int k = 0; k < h; k++) p1a += w[k];
+    for (int k = h + 1; k < L; k++) p1b += w[k];
+    for (int k = 0; k < h; k++) p2a += w[k] + w[k + 1];
+    for (int k = h; k < L - 1; k++) p2b += w[k] + w[k + 1];
+    if (h == L - 1) p2b += w[h];
+    const double t = std::max(p1a, p1b) + std::max(p2a, p2b);
+    if (t < best_t) {
+      best_t = t;
+      best = h;
+    }
+  }
+  return best;
 }
 
 }  // namespace
@@ -735,6 +911,12 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.zglob = (double*)workspace;
   a.z_in_smem = zs ? 1 : 0;
   a.cyclic = use_cyclic(c, cols) ? 1 : 0;
+  a.chains = 1;
+  a.split = 0;
+  if (a.cyclic && cols == c->N && off == 0 && c->N * c->N / 2 <= 32 && c->L >= 2 && use_two_chains()) {
+    a.chains = 2;
+    a.split = two_chain_split(*c);
+  }
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);

@@ -12,14 +12,16 @@ namespace sqg {
 constexpr int kTileMaxThreads = 256;
 constexpr int kTileMaxWarps = kTileMaxThreads / 32;
 
-// Applies one gate to every vector of the tile.
-__device__ __forceinline__ void tile_apply(double2* s, int N, int logN, int tc, const Gate& gt, const PairOp& op) {
+// Applies one gate to every vector of the tile; thread tid of nthr threads takes the
+// amplitude pairs tid, tid + nthr, ...
+__device__ __forceinline__ void tile_apply_by(double2* s, int N, int logN, int tc, const Gate& gt, const PairOp& op,
+                                              int tid, int nthr) {
   const bool ctrl = gate_controlled(gt.type);
   const int lognp = ctrl ? logN - 2 : logN - 1;
   const int npairs = 1 << lognp;
   const int items = tc << lognp;
   const int step = 1 << gt.target;
-  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+  for (int it = tid; it < items; it += nthr) {
     int col = it >> lognp;
     int p = it & (npairs - 1);
     int i = ctrl ? pair_index2(p, gt.target, gt.control) : pair_index1(p, gt.target);
@@ -29,6 +31,11 @@ __device__ __forceinline__ void tile_apply(double2* s, int N, int logN, int tc, 
     v[i] = x;
     v[i + step] = y;
   }
+}
+
+// Applies one gate to every vector of the tile (all threads of the CTA).
+__device__ __forceinline__ void tile_apply(double2* s, int N, int logN, int tc, const Gate& gt, const PairOp& op) {
+  tile_apply_by(s, N, logN, tc, gt, op, threadIdx.x, blockDim.x);
 }
 
 // Warp reduce-scatter of 8 doubles: afterwards lane l holds the warp total of value

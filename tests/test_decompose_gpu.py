@@ -19,13 +19,16 @@ def wl():
 @pytest.mark.parametrize("cols,offset,variant,form", [
     (8, 0, O.FROBENIUS_NORM, None), (8, 0, O.FROBENIUS_NORM, "sweep"), (6, 2, O.FROBENIUS_NORM, None),
     (4, 4, O.FROBENIUS_NORM, None), (4, 3, O.FROBENIUS_NORM, "cyclic"), (8, 0, O.HILBERT_SCHMIDT_TEST, None),
-    (8, 0, O.INFIDELITY, "sweep"), (8, 0, O.INFIDELITY, None)])
+    (8, 0, O.INFIDELITY, "sweep"), (8, 0, O.INFIDELITY, None), (8, 0, O.FROBENIUS_NORM, "onechain"),
+    (8, 0, O.HILBERT_SCHMIDT_TEST, "onechain")])
 def test_first_bfgs_steps_follow_the_oracle(sqg, wl, monkeypatch, cols, offset, variant, form):
     """With a small evaluation budget and no tolerance stop, the device BFGS lands where
     the oracle's restatement of BFGS_Powell lands: square and rectangular targets with a
     trace offset, all three cost variants, both forms of the device cost and gradient
-    (state sweeps, environment matrix)."""
-    if form:
+    (state sweeps, environment matrix carried by one warp or by two)."""
+    if form == "onechain":
+        monkeypatch.setenv("SQG_DECOMPOSE_CHAINS", "1")
+    elif form:
         monkeypatch.setenv("SQG_DECOMPOSE_FORM", form)
     n = 3
     rng = np.random.default_rng(41 + cols + offset + 10 * variant)
