@@ -134,11 +134,25 @@ def fp64_ops_per_eval(circuit_records, N, cols):
     return ops
 
 
-def fp64_ops_per_bfgs_iteration(P):
-    """FP64 thread instructions of one BFGS iteration of the device driver (decompose.cu):
-    Z^T g and Z(Z^T g) 2P^2, suffix sums P^2/2, Givens sweep 4P^2, Z^T gamma P^2, Z update
-    and column norms 2P^2, column rescaling at most P^2, plus O(P) vector work."""
-    return int(10.5 * P * P + 30 * P)
+def algorithmic_flops_per_eval(circuit_records, N, cols):
+    """Algorithmic FP64 flops of one cost + adjoint-gradient evaluation: three passes
+    (forward, left and right application) per parametric gate over the N x cols target,
+    16 flops per touched complex element (two complex multiply-adds); CRY touches the
+    control = 1 half; CNOT and CZ are exchanges and sign flips (no flops)."""
+    flops = 0
+    for t, tg, c, ps in circuit_records:
+        if t in (7, 8, 9, 10):
+            flops += 3 * 16 * N * cols
+        elif t == 14:
+            flops += 3 * 16 * N * cols // 2
+    return flops
+
+
+def bfgs_flops_per_iteration(P):
+    """Flops of one BFGS_Powell iteration of the reference algorithm
+    (BFGS_Powell.cpp:202-446): Z^T g 2P^2, Z (Z^T g) 2P^2, the Givens sweep 6P^2, Z^T gamma
+    2P^2, rank-one update 2P^2, column norms 2P^2, column scaling P^2."""
+    return 17 * P * P
 
 
 def bench_learned(sqg, wl, torch, ansatz, targets, tdev, plain_rate, plain_solved, steps):
@@ -242,10 +256,10 @@ def bench_ours(args):
     e2e_value = e2e_solved / sum(e2e_times)
     h2d = targets.nbytes + N_TARGETS * P * 8
     d2h = N_TARGETS * P * 8 + N_TARGETS * 8
-    # roofline of the decomposition kernel (FP64 pipe): algorithmic FP64 ops from the
-    # evaluations actually performed; BFGS linear algebra adds about 6 P^2 per iteration
-    ops_eval = fp64_ops_per_eval(ansatz.gate_records(), 8, 8)
-    achieved_tflops = 2.0 * (ops_eval * calls_tot + fp64_ops_per_bfgs_iteration(P) * iters_tot) / t_total / 1e12
+    # roofline of the decomposition kernel (FP64 pipe): algorithmic flops of the
+    # evaluations and BFGS iterations actually performed
+    flops_eval = algorithmic_flops_per_eval(ansatz.gate_records(), 8, 8)
+    achieved_tflops = (flops_eval * calls_tot + bfgs_flops_per_iteration(P) * iters_tot) / t_total / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -261,8 +275,10 @@ def bench_ours(args):
         "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
                      "peak_source": "measured live by the FP64 probe kernel",
                      "frac": achieved_tflops / FP64_PEAK_TFLOPS, "traffic": None,
-                     "note": "k_decompose is FP64-issue bound (ncu: FP64 pipe ~79% busy, HBM idle); achieved = "
-                             "model FP64 ops of the evaluations and BFGS iterations performed"},
+                     "note": "k_decompose is FP64-issue bound (HBM idle); achieved = algorithmic flops of the "
+                             "evaluations (3 passes x 16 flop per complex element per parametric gate) and BFGS "
+                             "iterations (17 P^2) performed, over the timed steps",
+                     "flops_per_eval": flops_eval, "flops_per_bfgs_iteration": bfgs_flops_per_iteration(P)},
         "bfgs_iterations_per_step": iters_tot / args.steps,
     }
     if not args.skip_learned:
