@@ -59,6 +59,8 @@ struct Sh {
   GateMat* gm;
   double* R;   // [L][8] reduced 2x2 overlaps of the reverse sweep
   int* pgate;  // gate owning each parameter
+  int* pg;     // indices of the parametric gates
+  int npg;
   double *x, *g, *d, *x0, *g0, *gbest, *ztg, *delta, *gamma, *gtz, *nz, *bestx, *guess, *S, *cs, *zs, *v, *vp, *sdv;
   double *Z, *redd, *tot, *scratch;
 };
@@ -114,29 +116,75 @@ __device__ void dec_build(const DecArgs& a, const Sh& sh, const double* xv) {
 __device__ double dec_finish(const DecArgs& a, const Sh& sh, double2 tr, double* gv) {
   const double* Rb = sh.R;
   double f;
-  const double dc = a.cols;
+  const double dc = a.cols, inv_dc = 1.0 / dc;
+  // x / cols and x * (1 / cols) round identically when cols is a power of two
+  const bool pow2 = (a.cols & (a.cols - 1)) == 0;
+  double cx = 0.0, cy = 0.0;  // HILBERT_SCHMIDT_TEST / INFIDELITY: grad = cx t.x - cy t.y
   if (a.variant == SQG_FROBENIUS_NORM) {
     f = 1.0 - tr.x / dc;
   } else if (a.variant == SQG_HILBERT_SCHMIDT_TEST) {
     double d = 1.0 / dc;
     f = 1.0 - d * d * (tr.x * tr.x + tr.y * tr.y);
+    cx = -2.0 * d * d * tr.x;
+    cy = 2.0 * d * d * tr.y;
   } else {
     f = 1.0 - ((tr.x * tr.x + tr.y * tr.y) / dc + 1) / (dc + 1);
+    cx = -2.0 / dc / (dc + 1) * tr.x;
+    cy = 2.0 / dc / (dc + 1) * tr.y;
   }
-  for (int p = threadIdx.x; p < a.P; p += blockDim.x) {
-    const int g = sh.pgate[p];
+  auto grad = [&](double tx, double ty) {
+    if (a.variant == SQG_FROBENIUS_NORM) return (1.0 - (pow2 ? tx * inv_dc : tx / dc)) - 1.0;
+    return cx * tx - cy * ty;
+  };
+  // one thread per parametric gate: the three U3 derivatives share their products and
+  // their kernels' zero entries (deriv_kernel) are skipped; the contractions keep the
+  // order of contract_derivative
+  for (int j = threadIdx.x; j < sh.npg; j += blockDim.x) {
+    const int g = sh.pg[j];
     const Gate gt = sh.gates[g];
-    double2 t = contract_derivative(gt, sh.sc, p - gt.pstart, Rb + g * 8);
-    double gvv;
-    if (a.variant == SQG_FROBENIUS_NORM) {
-      gvv = (1.0 - t.x / dc) - 1.0;
-    } else if (a.variant == SQG_HILBERT_SCHMIDT_TEST) {
-      double d = 1.0 / dc;
-      gvv = -2.0 * d * d * tr.x * t.x - 2.0 * d * d * tr.y * t.y;
+    const double* R = Rb + g * 8;
+    if (gt.type == G_U3) {
+      const double2* s3 = sh.sc + gt.pstart;
+      const double st = s3[0].x, ct = s3[0].y, sp = s3[1].x, cp = s3[1].y, sl = s3[2].x, cl = s3[2].y;
+      const double spl = sp * cl + cp * sl, cpl = cp * cl - sp * sl;
+      const double r0 = R[0], i0 = R[1], r1 = R[2], i1 = R[3], r2 = R[4], i2 = R[5], r3 = R[6], i3 = R[7];
+      // theta: (-st, 0), (-ct cl, -ct sl), (ct cp, ct sp), (-st cpl, -st spl)
+      double tx = -st * r0, ty = -st * i0;
+      double dx = -ct * cl, dy = -ct * sl;
+      tx = fma(dx, r1, fma(-dy, i1, tx));
+      ty = fma(dx, i1, fma(dy, r1, ty));
+      dx = ct * cp;
+      dy = ct * sp;
+      tx = fma(dx, r2, fma(-dy, i2, tx));
+      ty = fma(dx, i2, fma(dy, r2, ty));
+      dx = -st * cpl;
+      dy = -st * spl;
+      tx = fma(dx, r3, fma(-dy, i3, tx));
+      ty = fma(dx, i3, fma(dy, r3, ty));
+      gv[gt.pstart] = grad(tx, ty);
+      // phi: 0, 0, (-st sp, st cp), (-ct spl, ct cpl)
+      const double ex = -ct * spl, ey = ct * cpl;
+      dx = -st * sp;
+      dy = st * cp;
+      tx = fma(dx, r2, -dy * i2);
+      ty = fma(dx, i2, dy * r2);
+      tx = fma(ex, r3, fma(-ey, i3, tx));
+      ty = fma(ex, i3, fma(ey, r3, ty));
+      gv[gt.pstart + 1] = grad(tx, ty);
+      // lambda: 0, (st sl, -st cl), 0, (-ct spl, ct cpl)
+      dx = st * sl;
+      dy = -st * cl;
+      tx = fma(dx, r1, -dy * i1);
+      ty = fma(dx, i1, dy * r1);
+      tx = fma(ex, r3, fma(-ey, i3, tx));
+      ty = fma(ex, i3, fma(ey, r3, ty));
+      gv[gt.pstart + 2] = grad(tx, ty);
     } else {
-      gvv = -2.0 / dc / (dc + 1) * tr.x * t.x - 2.0 / dc / (dc + 1) * tr.y * t.y;
+      for (int k = 0; k < gate_param_num(gt.type); k++) {
+        const double2 t = contract_derivative(gt, sh.sc, k, R);
+        gv[gt.pstart + k] = grad(t.x, t.y);
+      }
     }
-    gv[p] = gvv;
   }
   __syncthreads();
   return f;
@@ -743,6 +791,13 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   sh.sc = (double2*)take(sizeof(double2) * max(P, 1));
   sh.R = (double*)take(sizeof(double) * 8 * max(L, 1));
   sh.pgate = (int*)take(sizeof(int) * max(P, 1));
+  sh.pg = (int*)take(sizeof(int) * max(L, 1));
+  sh.npg = 0;
+  for (int g = 0; g < L; g++)
+    if (gate_param_num(a.gates[g].type) > 0) {
+      if (threadIdx.x == 0) sh.pg[sh.npg] = g;
+      sh.npg++;
+    }
   double** vecs[] = {&sh.x, &sh.g, &sh.d, &sh.x0, &sh.g0, &sh.gbest, &sh.ztg, &sh.delta, &sh.gamma,
                      &sh.gtz, &sh.nz, &sh.bestx, &sh.guess, &sh.S, &sh.cs, &sh.zs, &sh.v, &sh.vp, &sh.sdv};
   static_assert(sizeof(vecs) / sizeof(vecs[0]) == kDecVectors, "dec_smem_bytes counts kDecVectors vectors");
@@ -801,7 +856,7 @@ size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem) {
   auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
   size_t s = r16(sizeof(Gate) * L) + 3 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
-             r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) +
+             r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) + r16(sizeof(int) * L) +
              kDecVectors * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
              r16(sizeof(double) * kTileMaxWarps);
   if (z_in_smem) s += r16(sizeof(double) * P * P);

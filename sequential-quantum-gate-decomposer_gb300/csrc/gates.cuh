@@ -105,6 +105,8 @@ struct PairOp {
 
 enum Orientation { ORIENT_FWD = 0, ORIENT_ADJ = 1, ORIENT_TRANS = 2, ORIENT_CONJ = 3 };
 
+// Sign flips go through dneg (an integer operation): a negated double that is stored,
+// rather than folded into the consuming FMA, would cost an FP64 instruction per gate.
 __device__ __forceinline__ PairOp make_op(int type, const GateMat& m, int orient) {
   PairOp op;
   op.kind = (type == G_CRY) ? G_RY : type;
@@ -116,23 +118,23 @@ __device__ __forceinline__ PairOp make_op(int type, const GateMat& m, int orient
   if (type == G_U3) {
     op.a = m.u[0].x;
     if (orient == ORIENT_ADJ) {  // [[u00, conj u10], [conj u01, conj u11]]
-      op.b = make_double2(m.u[2].x, -m.u[2].y);
-      op.c = make_double2(m.u[1].x, -m.u[1].y);
-      op.d = make_double2(m.u[3].x, -m.u[3].y);
+      op.b = make_double2(m.u[2].x, dneg(m.u[2].y));
+      op.c = make_double2(m.u[1].x, dneg(m.u[1].y));
+      op.d = make_double2(m.u[3].x, dneg(m.u[3].y));
     } else if (orient == ORIENT_TRANS) {  // [[u00, u10], [u01, u11]]
       op.b = m.u[2];
       op.c = m.u[1];
     } else if (orient == ORIENT_CONJ) {  // [[u00, conj u01], [conj u10, conj u11]]
-      op.b = make_double2(m.u[1].x, -m.u[1].y);
-      op.c = make_double2(m.u[2].x, -m.u[2].y);
-      op.d = make_double2(m.u[3].x, -m.u[3].y);
+      op.b = make_double2(m.u[1].x, dneg(m.u[1].y));
+      op.c = make_double2(m.u[2].x, dneg(m.u[2].y));
+      op.d = make_double2(m.u[3].x, dneg(m.u[3].y));
     }
   } else if (type == G_RY || type == G_CRY) {
     // RY^dagger = RY^T = RY(-theta); RY is real, so conj RY = RY
-    if (orient == ORIENT_ADJ || orient == ORIENT_TRANS) op.s = -op.s;
+    if (orient == ORIENT_ADJ || orient == ORIENT_TRANS) op.s = dneg(op.s);
   } else if (type == G_RX || type == G_RZ) {
     // RX, RZ are symmetric: RX^T = RX, RZ^T = RZ; adjoint and conjugate flip the sine.
-    if (orient == ORIENT_ADJ || orient == ORIENT_CONJ) op.s = -op.s;
+    if (orient == ORIENT_ADJ || orient == ORIENT_CONJ) op.s = dneg(op.s);
   }
   return op;
 }
