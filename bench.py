@@ -557,7 +557,7 @@ def bench_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def profile_case(case):
+def profile_case(case, profile_calls=60):
     """Small single-launch cases for ncu captures (one kernel of interest each)."""
     import torch
 
@@ -568,7 +568,8 @@ def profile_case(case):
         ansatz, targets = make_workload(sqg, wl)
         P = ansatz.get_Parameter_Num()
         B = 1216
-        dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=60, max_outer=1)
+        dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=profile_calls, max_outer=1,
+                                    stop_at_tolerance=profile_calls == 60)
         x, cost, calls = dec.run(torch.from_numpy(targets[:B]).cuda(), rng.uniform(0, 2 * np.pi, (B, P)))
     elif case == "gate_apply":
         c = wl.random_gate_circuit(12, 200, rng)
@@ -609,6 +610,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe-fp64", action="store_true", help="print the live FP64 FMA peak by active lanes")
     ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad", "mlp_gemm"], default=None)
+    ap.add_argument("--profile-calls", type=int, default=60,
+                    help="evaluations per BFGS run in the decompose profile case (below 60: no tolerance stop)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -624,7 +627,7 @@ def main():
         print(json.dumps({"fp64_fma_tflops_by_active_lanes": {k: native.probe_fp64_tflops(k) for k in (32, 16, 8, 1)}}))
         return
     if args.profile_case:
-        profile_case(args.profile_case)
+        profile_case(args.profile_case, args.profile_calls)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
