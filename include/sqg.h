@@ -189,6 +189,27 @@ int sqg_decompose_batched(const sqg_circuit* circuit, const void* targets_dev, i
                           int max_calls, int max_outer, int iteration_loops, int stop_at_tolerance,
                           unsigned long long seed, void* workspace_dev, size_t workspace_bytes, void* stream);
 
+/* Batched decompositions with SQUANDER's ADAM engine: replaces
+ * Optimization_Interface::solve_layer_optimization_problem_ADAM
+ * (src-cpp/optimization_engines/ADAM.cpp:44-330) with its Adam optimizer
+ * (src-cpp/common/Adam.cpp: beta1 0.68, beta2 0.8, epsilon 1e-4, local-minimum test) and
+ * randomize_parameters (src-cpp/decomposition/Optimization_Interface.cpp:576-607), the
+ * optimizer N_Qubit_Decomposition_custom selects above five qubits
+ * (N_Qubit_Decomposition_custom.cpp:59-76), here for qbit_num <= 5 with one CTA per target.
+ * Each target runs up to max_outer engine calls of at most max_iters cost+gradient
+ * evaluations (learning rate eta, adaptive as in the reference when adaptive_eta != 0, at
+ * most random_shift_count_max randomisations, randomisation after randomization_threshold
+ * evaluations without progress); it stops once the cost is below tolerance.  x (batch x P)
+ * holds the start points on entry and the best points on exit; cost receives the minimum,
+ * evals the evaluation count and shifts (nullable) the number of randomisations.  Random
+ * numbers come from a splitmix64 stream seeded with seed + 7919 b for target b.  Needs no
+ * workspace; asynchronous on stream. */
+int sqg_decompose_batched_adam(const sqg_circuit* circuit, const void* targets_dev, int cols, int batch,
+                               int trace_offset, int cost_variant, double* x_dev, double* cost_dev, int* evals_dev,
+                               int* shifts_dev, double tolerance, int max_iters, double eta, int adaptive_eta,
+                               int random_shift_count_max, long long randomization_threshold, int max_outer,
+                               unsigned long long seed, void* stream);
+
 /* Measures the FP64 FMA peak of the current device in TFLOP/s (an FMA counts 2 flops) with
  * independent DFMA chains on 8 CTAs per SM, timed with CUDA events; scratch_dev receives
  * the chains' results (sqg_probe_fp64_scratch_bytes() bytes).  With active_lanes < 32 only

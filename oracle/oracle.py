@@ -61,6 +61,8 @@ def lib():
                                         ctypes.c_uint64, dp, lp]
         _lib.sqgo_decompose_batch.argtypes = [i, ip, i, i, i, dp, i, i, i, dp, ctypes.c_double, ctypes.c_long, i,
                                               i, ctypes.c_uint64, dp, lp, i]
+        _lib.sqgo_adam_batch.argtypes = [i, ip, i, i, i, dp, i, i, i, dp, ctypes.c_double, ctypes.c_long,
+                                         ctypes.c_double, i, i, ctypes.c_long, ctypes.c_uint64, dp, lp, lp, i]
     return _lib
 
 
@@ -178,3 +180,25 @@ def decompose(qbit_num, gates, targets, x0, tolerance=1e-8, max_inner=10000, max
                                       _dp(costs), calls.ctypes.data_as(ctypes.POINTER(ctypes.c_long)), nthreads),
            "decompose")
     return x, costs, calls
+
+
+def adam_decompose(qbit_num, gates, targets, x0, tolerance=1e-8, max_iters=100000, eta=1e-3, adaptive_eta=True,
+                   random_shift_count_max=100, randomization_threshold=2500000, seed=0, nthreads=None,
+                   trace_offset=0, variant=FROBENIUS_NORM):
+    """SQUANDER's ADAM decomposition engine (optimization_engines/ADAM.cpp) of each target
+    (B, rows, cols) from the start points x0 (B, P).  Returns (x, minimum cost, evaluations,
+    randomisations)."""
+    g, gp, L = _gates(gates)
+    t = np.ascontiguousarray(targets, dtype=np.complex128)
+    x = np.array(x0, dtype=np.float64, order="C", copy=True)
+    B, P = x.shape
+    costs = np.zeros(B)
+    evals = np.zeros(B, dtype=np.int64)
+    shifts = np.zeros(B, dtype=np.int64)
+    nthreads = nthreads or os.cpu_count() or 1
+    _check(lib().sqgo_adam_batch(qbit_num, gp, L, P, B, _dp(t.view(np.float64)), t.shape[-1], trace_offset, variant,
+                                 _dp(x), tolerance, max_iters, eta, 1 if adaptive_eta else 0, random_shift_count_max,
+                                 randomization_threshold, seed, _dp(costs),
+                                 evals.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                                 shifts.ctypes.data_as(ctypes.POINTER(ctypes.c_long)), nthreads), "adam_decompose")
+    return x, costs, evals, shifts

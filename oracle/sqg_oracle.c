@@ -4,7 +4,7 @@
  * A plain-C restatement of the SQUANDER (rakytap/sequential-quantum-gate-decomposer)
  * decomposition hot path: parametric-circuit application to a 2^n x cols complex128
  * matrix, the FROBENIUS_NORM / HILBERT_SCHMIDT_TEST / INFIDELITY cost functions and
- * their gradients, the batched cost, and the BFGS (Powell-Z) decomposition driver.
+ * their gradients, the batched cost, and the BFGS (Powell-Z) and ADAM decomposition drivers.
  *
  * It is the checker for the CUDA engine (tests, smoke(), the CPU-baseline leg of
  * bench.py).  Nothing in the engine links or calls it.  Every routine follows the
@@ -18,6 +18,7 @@
  * counted in complex elements.  Qubit q is bit q of the row index (LSB = qubit 0),
  * src-cpp/gates/kernels/apply_kernel_to_input.cpp:52-67.
  */
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -699,6 +700,198 @@ int sqgo_decompose_batch(int qbit_num, const sqgo_gate* g, int L, int P, int B, 
   if (nthreads > 256) nthreads = 256;
   pthread_t th[256];
   for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, dec_worker, &j);
+  for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  pthread_mutex_destroy(&j.mu);
+  return 0;
+}
+
+/* ---------------- ADAM decomposition driver ----------------------------------------
+ * Optimization_Interface::solve_layer_optimization_problem_ADAM
+ * (optimization_engines/ADAM.cpp:44-330) with Adam::update (common/Adam.cpp:138-270),
+ * Adam::reset (:70-100), randomize_parameters (decomposition/Optimization_Interface.cpp:
+ * 576-607), the settings of set_optimizer(ADAM) (:1625-1628: random_shift_count_max 100)
+ * and the constructor defaults (adaptive_eta on, radius 1, randomization_rate 0.3, :56-64).
+ * Adam's bias-correction powers advance once per parameter, in parameter order (the
+ * reference advances them inside its parallel parameter loop).  Random numbers come from
+ * the seeded splitmix64 stream of the BFGS driver (the reference uses std::mt19937). */
+typedef struct {
+  double beta1, beta2, eps, eta;
+  double *mom, *var;
+  double beta1_t, beta2_t;
+  double f0_vec[100];
+  double f0_mean;
+  int f0_idx;
+  int dec_vec[20];
+  int dec_idx;
+  double dec_test, f0_prev;
+} adam_state;
+
+static void adam_reset(adam_state* a, int P) {
+  memset(a->mom, 0, sizeof(double) * P);
+  memset(a->var, 0, sizeof(double) * P);
+  a->beta1_t = 1.0;
+  a->beta2_t = 1.0;
+  memset(a->f0_vec, 0, sizeof(a->f0_vec));
+  a->f0_mean = 0.0;
+  a->f0_idx = 0;
+  for (int i = 0; i < 20; i++) a->dec_vec[i] = -1;
+  a->dec_idx = 0;
+  a->dec_test = -1.0;
+  a->f0_prev = DBL_MAX;
+}
+
+/* Returns 1 when the local-minimum test fires. */
+static int adam_update(adam_state* a, double* x, const double* g, double f0, int P) {
+  a->f0_mean = a->f0_mean + (f0 - a->f0_vec[a->f0_idx]) / 100;
+  a->f0_vec[a->f0_idx] = f0;
+  a->f0_idx = (a->f0_idx + 1) % 100;
+  double var_f0 = 0.0;
+  for (int i = 0; i < 100; i++) var_f0 = var_f0 + (a->f0_vec[i] - a->f0_mean) * (a->f0_vec[i] - a->f0_mean);
+  var_f0 = sqrt(var_f0) / 100;
+  if (f0 < a->f0_prev) {
+    if (a->dec_vec[a->dec_idx] != 1) a->dec_test = a->dec_test + 2.0 / 20;
+    a->dec_vec[a->dec_idx] = 1;
+  } else {
+    if (a->dec_vec[a->dec_idx] == 1) a->dec_test = a->dec_test - 2.0 / 20;
+    a->dec_vec[a->dec_idx] = -1;
+  }
+  a->dec_idx = (a->dec_idx + 1) % 20;
+  a->f0_prev = f0;
+  double grad_var = 0.0;
+  for (int i = 0; i < P; i++) grad_var += a->var[i];
+  const int barren = grad_var < a->eps && a->dec_test > 0.7;
+  const double eps = barren ? a->eps / 100 : a->eps;
+  for (int i = 0; i < P; i++) {
+    a->mom[i] = a->beta1 * a->mom[i] + (1 - a->beta1) * g[i];
+    a->var[i] = a->beta2 * a->var[i] + (1 - a->beta2) * g[i] * g[i];
+    a->beta1_t = a->beta1_t * a->beta1;
+    const double mh = a->mom[i] / (1 - a->beta1_t);
+    a->beta2_t = a->beta2_t * a->beta2;
+    const double vh = a->var[i] / (1 - a->beta2_t);
+    x[i] = x[i] - a->eta * mh / (sqrt(vh) + eps);
+  }
+  return (fabs(a->f0_mean - f0) < 1e-6 && a->dec_test <= 0.7 && var_f0 / a->f0_mean < 1e-6) ? 1 : 0;
+}
+
+int sqgo_adam_decompose(int qbit_num, const sqgo_gate* g, int L, int P, const double* target, int cols,
+                        int trace_offset, int variant, double* x, double tolerance, long max_iters, double eta,
+                        int adaptive_eta, int random_shift_count_max, long randomization_threshold, uint64_t seed,
+                        double* final_cost, long* evals, long* nshifts) {
+  int rc = check_gates(qbit_num, g, L, P);
+  if (rc) return rc;
+  fg_ctx c = {qbit_num, L, P, cols, trace_offset, variant, g, target, 0};
+  double* buf = (double*)malloc(sizeof(double) * 5 * (P > 0 ? P : 1));
+  double *xt = buf, *best = buf + P, *grad = buf + 2 * P;
+  adam_state a;
+  a.beta1 = 0.68; a.beta2 = 0.8; a.eps = 1e-4; a.eta = eta;  /* Adam.cpp:31-40, ADAM.cpp eta default 1e-3 */
+  a.mom = buf + 3 * P;
+  a.var = buf + 4 * P;
+  adam_reset(&a, P);
+  memcpy(xt, x, sizeof(double) * P);
+  memcpy(best, x, sizeof(double) * P);
+  double current_minimum = DBL_MAX, hold = DBL_MAX, f0 = DBL_MAX;
+  long sub_iter = 0, n = 0;
+  int shifts = 0, status = 0;
+  uint64_t s = seed;
+  for (long it = 0; it < max_iters; it++) {
+    fg_eval(&c, xt, &f0, grad);
+    n++;
+    if (sub_iter == 1) {
+      hold = f0;
+      if (adaptive_eta) a.eta = a.eta > 1e-3 ? a.eta : 1e-3;
+    }
+    if (hold * 0.95 > f0 || (hold * 0.97 > f0 && f0 < 1e-3) || (hold * 0.99 > f0 && f0 < 1e-4)) {
+      sub_iter = 0;
+      hold = f0;
+    }
+    if (current_minimum > f0) {
+      current_minimum = f0;
+      memcpy(best, xt, sizeof(double) * P);
+      if (adaptive_eta) {  /* the second clamp overwrites the first, as in the reference */
+        const double ne = 1e-3 * f0;
+        a.eta = ne > 1e-6 ? ne : 1e-6;
+        a.eta = ne < 1e-1 ? ne : 1e-1;
+      }
+    }
+    if (f0 < tolerance || shifts > random_shift_count_max) break;
+    if (sub_iter > randomization_threshold || status != 0) {
+      sub_iter = 0;
+      shifts++;
+      hold = current_minimum;
+      const double r = sqrt(f0);
+      for (int j = 0; j < P; j++) {
+        const double u = (double)(splitmix(&s) >> 11) * (1.0 / 9007199254740992.0);
+        if (u <= 0.3) {
+          const double w = (double)(splitmix(&s) >> 11) * (1.0 / 9007199254740992.0);
+          xt[j] = best[j] + (-2 * M_PI + 4 * M_PI * w) * r * 1.0;
+        } else {
+          xt[j] = best[j];
+        }
+      }
+      adam_reset(&a, P);
+      status = 0;
+    } else {
+      status = adam_update(&a, xt, grad, f0, P);
+    }
+    sub_iter++;
+  }
+  memcpy(x, best, sizeof(double) * P);
+  *final_cost = current_minimum;
+  if (evals) *evals = n;
+  if (nshifts) *nshifts = shifts;
+  free(buf);
+  return 0;
+}
+
+typedef struct {
+  int qbit_num, L, P, cols, trace_offset, variant, B, adaptive_eta, random_shift_count_max;
+  const sqgo_gate* g;
+  const double* targets;
+  double* x;
+  double tolerance, eta;
+  long max_iters, randomization_threshold;
+  uint64_t seed;
+  double* cost;
+  long *evals, *shifts;
+  int next;
+  pthread_mutex_t mu;
+} adam_job;
+
+static void* adam_worker(void* arg) {
+  adam_job* j = (adam_job*)arg;
+  size_t tsz = (size_t)2 * (1 << j->qbit_num) * j->cols;
+  for (;;) {
+    pthread_mutex_lock(&j->mu);
+    int b = j->next++;
+    pthread_mutex_unlock(&j->mu);
+    if (b >= j->B) break;
+    sqgo_adam_decompose(j->qbit_num, j->g, j->L, j->P, j->targets + tsz * b, j->cols, j->trace_offset, j->variant,
+                        j->x + (size_t)b * j->P, j->tolerance, j->max_iters, j->eta, j->adaptive_eta,
+                        j->random_shift_count_max, j->randomization_threshold, j->seed + (uint64_t)b * 7919u,
+                        &j->cost[b], &j->evals[b], &j->shifts[b]);
+  }
+  return NULL;
+}
+
+/* B independent ADAM decompositions spread over nthreads threads (seed + 7919 b each). */
+int sqgo_adam_batch(int qbit_num, const sqgo_gate* g, int L, int P, int B, const double* targets, int cols,
+                    int trace_offset, int variant, double* x, double tolerance, long max_iters, double eta,
+                    int adaptive_eta, int random_shift_count_max, long randomization_threshold, uint64_t seed,
+                    double* cost, long* evals, long* shifts, int nthreads) {
+  int rc = check_gates(qbit_num, g, L, P);
+  if (rc) return rc;
+  adam_job j;
+  memset(&j, 0, sizeof(j));
+  j.qbit_num = qbit_num; j.L = L; j.P = P; j.cols = cols; j.trace_offset = trace_offset; j.variant = variant;
+  j.B = B; j.adaptive_eta = adaptive_eta; j.random_shift_count_max = random_shift_count_max; j.g = g;
+  j.targets = targets; j.x = x; j.tolerance = tolerance; j.eta = eta; j.max_iters = max_iters;
+  j.randomization_threshold = randomization_threshold; j.seed = seed; j.cost = cost; j.evals = evals;
+  j.shifts = shifts;
+  pthread_mutex_init(&j.mu, NULL);
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, adam_worker, &j);
   for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
   pthread_mutex_destroy(&j.mu);
   return 0;

@@ -1,9 +1,10 @@
 """Batched decompositions on the device (one BFGS decomposition per CTA, one launch).
 
 This is the throughput form of SQUANDER's ``N_Qubit_Decomposition_custom`` with the
-BFGS optimizer (src-cpp/decomposition/N_Qubit_Decomposition_custom.cpp:116-190): every
-target of the batch is decomposed with the same gate structure, each from its own start
-point, without a host round trip per iteration.
+BFGS optimizer (src-cpp/decomposition/N_Qubit_Decomposition_custom.cpp:116-190) or its
+ADAM engine (src-cpp/optimization_engines/ADAM.cpp:44-330): every target of the batch is
+decomposed with the same gate structure, each from its own start point, without a host
+round trip per iteration.
 """
 import numpy as np
 
@@ -16,8 +17,20 @@ class BatchedDecomposer:
     """Decomposes batches of targets (each given as U^dagger) with one gate structure."""
 
     def __init__(self, circuit, tolerance=1e-8, max_calls=10000, max_outer=4, iteration_loops=1,
-                 stop_at_tolerance=True, trace_offset=0, cost_variant=0):
+                 stop_at_tolerance=True, trace_offset=0, cost_variant=0, optimizer="BFGS", eta=1e-3,
+                 adaptive_eta=True, random_shift_count_max=100, randomization_threshold=2500000):
+        """optimizer "BFGS": BFGS_Powell runs of at most max_calls evaluations each, restarted
+        iteration_loops times per outer iteration.  optimizer "ADAM": one ADAM engine call of at
+        most max_calls evaluations per outer iteration (SQUANDER sets max_outer_iterations 1,
+        max_inner_iterations 100000 and random_shift_count_max 100 for ADAM)."""
         dev.require_cuda()
+        self.optimizer = str(optimizer).upper()
+        if self.optimizer not in ("BFGS", "ADAM"):
+            raise ValueError("optimizer must be BFGS or ADAM")
+        self.eta = float(eta)
+        self.adaptive_eta = bool(adaptive_eta)
+        self.random_shift_count_max = int(random_shift_count_max)
+        self.randomization_threshold = int(randomization_threshold)
         if not isinstance(circuit, Circuit):
             raise TypeError("circuit must be a Circuit")
         self.circuit = circuit
@@ -34,7 +47,7 @@ class BatchedDecomposer:
     def run(self, targets_udag, x0, seed=0, stream=None):
         """targets_udag: (B, rows, cols) complex128; x0: (B, P) float64 (host or device).
         Returns CUDA tensors (x (B, P), cost (B,), calls (B,) int32); asynchronous.  The BFGS
-        iteration counts of the call are left in self.iters."""
+        iteration counts (ADAM: randomisation counts) of the call are left in self.iters."""
         t = dev.to_device_complex(targets_udag)
         if t.dim() != 3 or t.shape[1] != (1 << self.native.qbit_num):
             raise ValueError("targets must be (B, 2**qbit_num, cols)")
@@ -46,6 +59,14 @@ class BatchedDecomposer:
         calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
         self.iters = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
         lib = _native.lib()
+        if self.optimizer == "ADAM":
+            _native.check(lib.sqg_decompose_batched_adam(
+                self.native.handle, dev.ptr(t), cols, B, self.trace_offset, self.cost_variant, dev.ptr(x),
+                dev.ptr(cost), dev.ptr(calls), dev.ptr(self.iters), self.tolerance, self.max_calls, self.eta,
+                1 if self.adaptive_eta else 0, self.random_shift_count_max, self.randomization_threshold,
+                self.max_outer, int(seed) & 0xFFFFFFFFFFFFFFFF, dev.stream_ptr(stream)), "sqg_decompose_batched_adam")
+            self._keep = t
+            return x, cost, calls
         ws = self._ws.get(lib.sqg_decompose_workspace_bytes(self.native.handle, B, cols))
         _native.check(lib.sqg_decompose_batched(
             self.native.handle, dev.ptr(t), cols, B, self.trace_offset, self.cost_variant, dev.ptr(x), dev.ptr(cost),

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cstdlib>
 #include <string>
 
@@ -50,7 +51,13 @@ struct DecArgs {
   int cyclic;  // cost and gradient through the environment matrix (dec_eval_cyclic)
   int chains;  // 2: the two-warp form dec_eval_cyclic2, split at gate `split`
   int split;
+  // ADAM engine (k_decompose<kAdam>)
+  double eta;
+  int adaptive_eta, shift_max;
+  long long rand_thr;
 };
+
+enum { kBfgs = 0, kAdam = 1 };
 
 struct Sh {
   const Gate* gates;    // shared-memory copy of the gate list
@@ -770,9 +777,154 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
   return f;
 }
 
+__device__ __forceinline__ unsigned long long splitmix_step(unsigned long long& s) {
+  s += 0x9E3779B97F4A7C15ULL;
+  unsigned long long z = s;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double splitmix_u01(unsigned long long& s) {
+  return (double)(splitmix_step(s) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// SQUANDER's ADAM engine for one target (Optimization_Interface::
+// solve_layer_optimization_problem_ADAM, optimization_engines/ADAM.cpp:44-330) with its Adam
+// optimizer (common/Adam.cpp: beta1 0.68, beta2 0.8, epsilon 1e-4; reset :70-100, update
+// :138-270) and randomize_parameters (decomposition/Optimization_Interface.cpp:576-607:
+// 30% of the parameters moved by U(-2 pi, 2 pi) * sqrt(f) around the best point).  The scalar
+// bookkeeping is replicated in every thread; thread 0 draws the random numbers from the
+// target's splitmix64 stream.  Adam's bias-correction powers advance once per parameter in
+// parameter order, as in the reference; pw1/pw2 hold beta^(i + 1).  Starts from sh.x, leaves
+// the best point in sh.bestx and returns the minimum.
+__device__ double dec_adam(const DecArgs& a, const Sh& sh, int b, int& calls, int& shifts, double cur_min,
+                           unsigned long long& rng, double* f0_vec, int* dec_vec) {
+  const int P = a.P;
+  double *xt = sh.x, *g = sh.g, *best = sh.bestx, *mom = sh.v, *var = sh.vp, *pw1 = sh.S, *pw2 = sh.sdv;
+  const double b1 = 0.68, b2 = 0.8, aeps = 1e-4, kPi = 3.14159265358979323846;
+  if (threadIdx.x == 0) {
+    double t1 = 1.0, t2 = 1.0;
+    for (int i = 0; i < P; i++) {
+      t1 = t1 * b1;
+      t2 = t2 * b2;
+      pw1[i] = t1;
+      pw2[i] = t2;
+    }
+  }
+  double eta = a.eta;
+  double beta1_t = 1.0, beta2_t = 1.0, f0_mean = 0.0, dec_test = -1.0, f0_prev = DBL_MAX;
+  int f0_idx = 0, dec_idx = 0;
+  auto reset_arrays = [&]() {
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      mom[i] = 0.0;
+      var[i] = 0.0;
+    }
+    for (int i = threadIdx.x; i < 100; i += blockDim.x) f0_vec[i] = 0.0;
+    for (int i = threadIdx.x; i < 20; i += blockDim.x) dec_vec[i] = -1;
+  };
+  reset_arrays();
+  for (int i = threadIdx.x; i < P; i += blockDim.x) best[i] = xt[i];
+  __syncthreads();
+  double hold = cur_min;
+  long long sub_iter = 0;
+  int status = 0, shift_cnt = 0;  // random_shift_count of this engine call
+  for (int it = 0; it < a.max_calls; it++) {
+    const double f0 = dec_eval(a, sh, xt, g, b);
+    calls++;
+    if (sub_iter == 1) {
+      hold = f0;
+      if (a.adaptive_eta) eta = eta > 1e-3 ? eta : 1e-3;
+    }
+    if (hold * 0.95 > f0 || (hold * 0.97 > f0 && f0 < 1e-3) || (hold * 0.99 > f0 && f0 < 1e-4)) {
+      sub_iter = 0;
+      hold = f0;
+    }
+    if (cur_min > f0) {
+      cur_min = f0;
+      for (int i = threadIdx.x; i < P; i += blockDim.x) best[i] = xt[i];
+      if (a.adaptive_eta) {  // the second clamp overwrites the first, as in the reference
+        const double ne = 1e-3 * f0;
+        eta = ne > 1e-6 ? ne : 1e-6;
+        eta = ne < 1e-1 ? ne : 1e-1;
+      }
+    }
+    if (f0 < a.tol || shift_cnt > a.shift_max) break;
+    if (sub_iter > a.rand_thr || status != 0) {
+      sub_iter = 0;
+      shift_cnt++;
+      hold = cur_min;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const double r = sqrt(f0);
+        for (int j = 0; j < P; j++) {
+          if (splitmix_u01(rng) <= 0.3)
+            xt[j] = best[j] + (-2 * kPi + 4 * kPi * splitmix_u01(rng)) * r * 1.0;
+          else
+            xt[j] = best[j];
+        }
+      }
+      beta1_t = 1.0;
+      beta2_t = 1.0;
+      f0_mean = 0.0;
+      f0_idx = 0;
+      dec_idx = 0;
+      dec_test = -1.0;
+      f0_prev = DBL_MAX;
+      reset_arrays();
+      status = 0;
+      __syncthreads();
+    } else {
+      f0_mean = f0_mean + (f0 - f0_vec[f0_idx]) / 100;
+      int dv = dec_vec[dec_idx];
+      __syncthreads();  // every thread has read the entries rewritten below
+      if (threadIdx.x == 0) f0_vec[f0_idx] = f0;
+      f0_idx = (f0_idx + 1) % 100;
+      if (f0 < f0_prev) {
+        if (dv != 1) dec_test = dec_test + 2.0 / 20;
+        dv = 1;
+      } else {
+        if (dv == 1) dec_test = dec_test - 2.0 / 20;
+        dv = -1;
+      }
+      if (threadIdx.x == 0) dec_vec[dec_idx] = dv;
+      dec_idx = (dec_idx + 1) % 20;
+      f0_prev = f0;
+      double red[2] = {0.0, 0.0};
+      __syncthreads();  // the new window entry is visible below
+      for (int i = threadIdx.x; i < 100; i += blockDim.x) {
+        const double d = f0_vec[i] - f0_mean;
+        red[0] = fma(d, d, red[0]);
+      }
+      for (int i = threadIdx.x; i < P; i += blockDim.x) red[1] += var[i];
+      block_allsum_n(red, sh.redd);
+      const double var_f0 = sqrt(red[0]) / 100, grad_var = red[1];
+      const double eps = (grad_var < aeps && dec_test > 0.7) ? aeps / 100 : aeps;
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const double gi = g[i];
+        const double m = b1 * mom[i] + (1 - b1) * gi;
+        const double v = b2 * var[i] + (1 - b2) * gi * gi;
+        mom[i] = m;
+        var[i] = v;
+        const double mh = m / (1 - beta1_t * pw1[i]);
+        const double vh = v / (1 - beta2_t * pw2[i]);
+        xt[i] = xt[i] - eta * mh / (sqrt(vh) + eps);
+      }
+      beta1_t = beta1_t * pw1[P - 1];
+      beta2_t = beta2_t * pw2[P - 1];
+      status = (fabs(f0_mean - f0) < 1e-6 && dec_test <= 0.7 && var_f0 / f0_mean < 1e-6) ? 1 : 0;
+      __syncthreads();
+    }
+    sub_iter++;
+  }
+  __syncthreads();
+  shifts += shift_cnt;
+  return cur_min;
+}
+
 // At most 80 registers (6 CTAs of 128 threads per SM): the evaluation keeps only one warp
 // per CTA busy at n = 3, so resident CTAs are what hides FP64 and shared-memory latency
 // (measured 7470 vs 7103 decompositions/s with the unconstrained 126 registers).
+template <int OPT>
 __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   extern __shared__ double2 smem2[];
   const int b = blockIdx.x;
@@ -805,7 +957,15 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   sh.redd = (double*)take(sizeof(double) * kTileMaxWarps * 8);
   sh.tot = (double*)take(sizeof(double) * 8);
   sh.scratch = (double*)take(sizeof(double) * kTileMaxWarps);
-  sh.Z = a.z_in_smem ? (double*)take(sizeof(double) * P * P) : a.zglob + (long long)b * P * P;
+  double* f0_vec = nullptr;
+  int* dec_vec = nullptr;
+  if (OPT == kAdam) {
+    f0_vec = (double*)take(sizeof(double) * 100);
+    dec_vec = (int*)take(sizeof(int) * 20);
+    sh.Z = nullptr;
+  } else {
+    sh.Z = a.z_in_smem ? (double*)take(sizeof(double) * P * P) : a.zglob + (long long)b * P * P;
+  }
 
   for (int e = threadIdx.x; e < NC; e += blockDim.x) tsh[e] = a.targets[(long long)b * a.tstride + e];
   for (int g = threadIdx.x; g < L; g += blockDim.x) {
@@ -817,8 +977,23 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   __syncthreads();
   double best = INFINITY;
   int calls = 0, iters = 0;
+  if (OPT == kAdam) {
+    // one engine call per outer iteration from the best point so far, the running minimum
+    // carried over (Decomposition_Base keeps current_minimum across them)
+    unsigned long long rng = a.seed + (unsigned long long)b * 7919ULL;
+    double cur_min = DBL_MAX;
+    for (int outer = 0; outer < a.max_outer; outer++) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.guess[i];
+      __syncthreads();
+      cur_min = dec_adam(a, sh, b, calls, iters, cur_min, rng, f0_vec, dec_vec);
+      for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = sh.bestx[i];
+      __syncthreads();
+      if (fabs(cur_min) < a.tol) break;
+    }
+    best = cur_min;
+  }
   unsigned long long ctr = a.seed * 0x2545F4914F6CDD1DULL + (unsigned long long)b * 0x9E3779B97F4A7C15ULL;
-  bool done = false;
+  bool done = OPT == kAdam;
   for (int outer = 0; outer < a.max_outer && !done; outer++) {
     for (int loop = 0; loop < a.loops; loop++) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.guess[i];
@@ -852,13 +1027,14 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   }
 }
 
-size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem) {
+size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem, bool adam = false) {
   auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
   size_t s = r16(sizeof(Gate) * L) + 3 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
              r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) + r16(sizeof(int) * L) +
              kDecVectors * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
              r16(sizeof(double) * kTileMaxWarps);
+  if (adam) return s + r16(sizeof(double) * 100) + r16(sizeof(int) * 20);
   if (z_in_smem) s += r16(sizeof(double) * P * P);
   return s;
 }
@@ -920,6 +1096,35 @@ int two_chain_split(const sqg_circuit& c) {
   return best;
 }
 
+// Kernel attributes and launch shared by the BFGS and ADAM entry points.
+template <int OPT>
+int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess && smem > (size_t)optin)
+    return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
+  // raised to the device maximum, never lowered: the attribute is shared by all callers
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_decompose<OPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  // one thread per parameter for the vector and Z-matrix work, at least two warps
+  const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
+  k_decompose<OPT><<<batch, threads, smem, (cudaStream_t)stream>>>(a);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
+}
+
+// Evaluation form of the decomposition kernels for this circuit and target width.
+void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
+  a.cyclic = use_cyclic(c, cols) ? 1 : 0;
+  a.chains = 1;
+  a.split = 0;
+  if (a.cyclic && cols == c->N && off == 0 && c->N * c->N / 2 <= 32 && c->L >= 2 && use_two_chains()) {
+    a.chains = 2;
+    a.split = two_chain_split(*c);
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -950,7 +1155,7 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   if (smem > 227 * 1024) return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
   if (!zs && (!workspace || ws_bytes < (size_t)batch * c->P * c->P * sizeof(double)))
     return set_error(SQG_ERR_WORKSPACE, "workspace too small for the per-instance BFGS matrices");
-  DecArgs a;
+  DecArgs a = {};
   a.gates = c->d_gates;
   a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N; a.cols = cols;
   a.trace_offset = off;
@@ -965,26 +1170,49 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.seed = seed;
   a.zglob = (double*)workspace;
   a.z_in_smem = zs ? 1 : 0;
-  a.cyclic = use_cyclic(c, cols) ? 1 : 0;
-  a.chains = 1;
-  a.split = 0;
-  if (a.cyclic && cols == c->N && off == 0 && c->N * c->N / 2 <= 32 && c->L >= 2 && use_two_chains()) {
-    a.chains = 2;
-    a.split = two_chain_split(*c);
-  }
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (e == cudaSuccess && smem > (size_t)optin)
-    return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
-  // raised to the device maximum, never lowered: the attribute is shared by all callers
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_decompose, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-  // one thread per parameter for the vector and Z-matrix work, at least two warps
-  const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
-  k_decompose<<<batch, threads, smem, (cudaStream_t)stream>>>(a);
-  e = cudaGetLastError();
-  return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
+  dec_eval_form(c, cols, off, a);
+  return dec_launch<kBfgs>(c, a, batch, smem, stream);
+}
+
+
+int sqg_decompose_batched_adam(const sqg_circuit* c, const void* targets, int cols, int batch, int trace_offset,
+                               int cost_variant, double* x, double* cost, int* evals, int* shifts, double tolerance,
+                               int max_iters, double eta, int adaptive_eta, int random_shift_count_max,
+                               long long randomization_threshold, int max_outer, unsigned long long seed,
+                               void* stream) {
+  if (!c || !targets || !x || !cost || !evals || batch <= 0 || batch > 0x7fffffff / 2 || cols <= 0 || cols > c->N)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "bad circuit, batch, targets or outputs");
+  if (c->P == 0) return set_error(SQG_ERR_INVALID_ARGUMENT, "the circuit has no free parameters");
+  if (cost_variant != SQG_FROBENIUS_NORM && cost_variant != SQG_HILBERT_SCHMIDT_TEST && cost_variant != SQG_INFIDELITY)
+    return set_error(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
+  const int off = cost_variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
+  if (off < 0 || off + cols > c->N) return set_error(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
+  if (c->n > 5) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 5");
+  if (max_iters < 1 || max_outer < 1 || random_shift_count_max < 0 || randomization_threshold < 0)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
+  const size_t smem = dec_smem_bytes(c, cols, false, true);
+  if (smem > 227 * 1024) return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
+  DecArgs a = {};
+  a.gates = c->d_gates;
+  a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N; a.cols = cols;
+  a.trace_offset = off;
+  a.variant = cost_variant;
+  a.targets = (const double2*)targets;
+  a.tstride = (long long)c->N * cols;
+  a.x = x; a.cost = cost; a.calls = evals; a.iters = shifts;
+  a.B = batch;
+  a.tol = tolerance;
+  a.max_calls = max_iters; a.max_outer = max_outer; a.loops = 1;
+  a.early_stop = 1;
+  a.seed = seed;
+  a.zglob = nullptr;
+  a.z_in_smem = 0;
+  a.eta = eta;
+  a.adaptive_eta = adaptive_eta ? 1 : 0;
+  a.shift_max = random_shift_count_max;
+  a.rand_thr = randomization_threshold;
+  dec_eval_form(c, cols, off, a);
+  return dec_launch<kAdam>(c, a, batch, smem, stream);
 }
 
 }  // extern "C"

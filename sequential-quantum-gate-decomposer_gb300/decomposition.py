@@ -16,7 +16,7 @@ import numpy as np
 from . import _device as dev
 from .circuit import Circuit, combined_unitary_device
 from .evaluator import FROBENIUS_NORM, SUPPORTED_VARIANTS, CostEvaluator
-from .optim import adam, bfgs_powell
+from .optim import adam_squander, bfgs_powell
 
 _GUESS = {"zeros": "ZEROS", "random": "RANDOM", "close_to_zero": "CLOSE_TO_ZERO"}
 
@@ -233,15 +233,29 @@ class N_Qubit_Decomposition_custom:
         guess = self._initial(P)
         best_x, best_f = guess.copy(), math.inf
         for _outer in range(max_outer):
-            for _loop in range(loops):
-                if self.optimizer == "BFGS":
-                    f, calls = bfgs_powell(self._fg, guess, max_inner)
-                else:
-                    f, calls = adam(self._fg, guess, max_inner, tol=tol)
+            if self.optimizer == "ADAM":
+                # solve_layer_optimization_problem_ADAM (optimization_engines/ADAM.cpp:44-330); the
+                # config lookups keep the reference's precedence (an "eta" or "adaptive_eta" key
+                # decides over its "_adam" variant, ADAM.cpp:150-185)
+                cfg = self.config
+                eta = float(cfg["eta"]) if "eta" in cfg else 1e-3
+                adaptive = bool(cfg["adaptive_eta"]) if "adaptive_eta" in cfg else True
+                thr = int(cfg.get("randomization_threshold_adam", cfg.get("randomization_threshold", 2500000)))
+                tol_a = float(cfg.get("optimization_tolerance_adam", tol))
+                x = guess.copy()
+                f, calls = adam_squander(self._fg, x, max_inner, tol_a, eta, adaptive,
+                                         int(cfg.get("random_shift_count_max", 100)), thr,
+                                         seed=int(self.rng.integers(1 << 62)), current_minimum=best_f)
                 self.num_iters += calls
                 if f < best_f:
-                    best_f, best_x = f, guess.copy()
-                    guess += self.rng.uniform(0.0, 2 * math.pi, P) / 100
+                    best_f, best_x = f, x.copy()
+            else:
+                for _loop in range(loops):
+                    f, calls = bfgs_powell(self._fg, guess, max_inner)
+                    self.num_iters += calls
+                    if f < best_f:
+                        best_f, best_x = f, guess.copy()
+                        guess += self.rng.uniform(0.0, 2 * math.pi, P) / 100
             guess = best_x.copy()
             if abs(best_f) < tol:
                 break

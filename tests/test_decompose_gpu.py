@@ -118,3 +118,49 @@ def test_every_restart_gets_its_own_budget(sqg, wl):
     assert np.all(calls > max_calls)  # the restarts ran
     _, _, callr = O.decompose(n, c.gate_records(), targets, x0, tolerance=1e-8, max_inner=max_calls, max_outer=outer)
     assert np.all(callr > max_calls) and np.all(callr <= outer * max_calls)
+
+
+def _one_cnot_circuit(sqg):
+    c = sqg.Circuit(2)
+    c.add_U3(0)
+    c.add_U3(1)
+    c.add_CNOT(1, 0)
+    c.add_U3(0)
+    c.add_U3(1)
+    return c
+
+
+@pytest.mark.parametrize("case", ["fit2", "exact3"])
+def test_device_adam_follows_the_oracle(sqg, wl, case):
+    """k_decompose with SQUANDER's ADAM engine against the oracle's restatement of it: the
+    same evaluation counts, the same randomisations (the local-minimum test fires on the
+    two-qubit one-CNOT fit to Haar targets) and the same trajectory to rounding."""
+    rng = np.random.default_rng(77)
+    if case == "fit2":
+        n, c, iters, adaptive = 2, _one_cnot_circuit(sqg), 3000, False
+        targets = np.stack([np.ascontiguousarray(wl.haar_unitary(4, rng).conj().T) for _ in range(8)])
+    else:
+        n, c, iters, adaptive = 3, wl.cnot_u3_ansatz(3, 4), 400, True
+        P = c.get_Parameter_Num()
+        targets = np.stack([np.ascontiguousarray(O.get_matrix(3, c.gate_records(), rng.uniform(0, 2 * np.pi, P)).conj().T)
+                            for _ in range(8)])
+    P = c.get_Parameter_Num()
+    x0 = rng.uniform(0, 2 * np.pi, (targets.shape[0], P))
+    dec = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=iters, max_outer=1, optimizer="ADAM", eta=1e-3,
+                                adaptive_eta=adaptive)
+    x, cost, evals = dec.run(targets, x0, seed=4)
+    torch.cuda.synchronize()
+    xr, cr, er, sr = O.adam_decompose(n, c.gate_records(), targets, x0, tolerance=1e-8, max_iters=iters, eta=1e-3,
+                                      adaptive_eta=adaptive, seed=4)
+    shifts = dec.iters.cpu().numpy()
+    same = shifts == sr
+    assert same.sum() >= targets.shape[0] - 1, (shifts, sr)
+    assert np.array_equal(evals.cpu().numpy()[same], er[same])
+    if case == "fit2":
+        # after a randomisation, rounding-level differences of the cost move the iteration at
+        # which the next local-minimum test fires; both land in the same minimum
+        assert sr.max() >= 1  # the randomisation branch ran
+        assert np.allclose(cost.cpu().numpy()[same], cr[same], rtol=1e-4)
+    else:
+        assert np.allclose(cost.cpu().numpy(), cr, rtol=1e-9, atol=1e-12)
+        assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)

@@ -83,6 +83,47 @@ def test_host_bfgs_matches_oracle_driver(sqg):
     assert np.allclose(x_host, x_or[0], atol=1e-9)
 
 
+@pytest.mark.parametrize("adaptive,eta", [(False, 1e-3), (True, 1e-3)])
+def test_host_adam_matches_oracle_engine(sqg, adaptive, eta):
+    """The host restatement of SQUANDER's ADAM engine (optim.adam_squander) and the oracle's
+    C restatement follow the same path, randomisations included, on the same cost function:
+    a two-qubit fit with one CNOT to a Haar-random target, whose local minima make the
+    engine's local-minimum test fire."""
+    optim = importlib.import_module("sequential-quantum-gate-decomposer_gb300.optim")
+    wl = importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+    c = sqg.Circuit(2)
+    c.add_U3(0)
+    c.add_U3(1)
+    c.add_CNOT(1, 0)
+    c.add_U3(0)
+    c.add_U3(1)
+    recs = c.gate_records()
+    rng = np.random.default_rng(9)
+    T = np.ascontiguousarray(wl.haar_unitary(4, rng).conj().T)
+    x0 = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    x = x0.copy()
+    info = {}
+    f, n = optim.adam_squander(lambda th: O.cost_grad(2, recs, th, T), x, max_iters=3000, tol=1e-8, eta=eta,
+                               adaptive_eta=adaptive, seed=4, info=info)
+    xr, cr, er, sr = O.adam_decompose(2, recs, T[None], x0[None], tolerance=1e-8, max_iters=3000, eta=eta,
+                                      adaptive_eta=adaptive, seed=4)
+    assert n == er[0] and info["shifts"] == sr[0]
+    assert f == cr[0] and np.array_equal(x, xr[0])
+    if not adaptive:
+        assert sr[0] >= 1  # the randomisation branch ran
+
+
+def test_adam_state_bias_correction_order():
+    """Adam.cpp advances beta1_t and beta2_t once per parameter inside its update loop."""
+    optim = importlib.import_module("sequential-quantum-gate-decomposer_gb300.optim")
+    st = optim.AdamState(3, 0.1)
+    x = np.zeros(3)
+    st.update(x, np.ones(3), 1.0)
+    assert st.beta1_t == 0.68 * 0.68 * 0.68 and st.beta2_t == 0.8 * 0.8 * 0.8
+    # first component: bias-corrected moments (1 - b) g / (1 - b) = g, so the step is eta / (1 + eps)
+    assert x[0] == pytest.approx(-0.1 / (1 + 1e-4), rel=1e-15)
+
+
 def test_engine_fails_loudly_without_gpu(sqg):
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():
