@@ -301,3 +301,32 @@ def test_circuits_without_gates_or_parameters(sqg, kind):
     assert grad.shape == (2, 0)
     assert np.allclose(c.get_Matrix(np.zeros(0)), O.get_matrix(n, c.gate_records(), np.zeros(0)), atol=1e-14)
     assert c.apply_derivate_to(np.zeros(0), np.eye(8, dtype=np.complex128)) == []
+
+
+def test_dropin_adam_above_five_qubits_follows_the_oracle(sqg):
+    """N_Qubit_Decomposition_custom picks ADAM for qbit_num > 5 (N_Qubit_Decomposition_custom.cpp:
+    59-76); its engine driven by the GPU cost and gradient follows the same engine driven by
+    the oracle."""
+    import importlib
+
+    optim = importlib.import_module("sequential-quantum-gate-decomposer_gb300.optim")
+    wl = importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+    n = 6
+    rng = np.random.default_rng(66)
+    c = wl.cnot_u3_ansatz(n, 6)
+    P = c.get_Parameter_Num()
+    U = O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, P))
+    T = np.ascontiguousarray(U.conj().T)
+    dec = sqg.N_Qubit_Decomposition_custom(T, config={"max_inner_iterations": 200, "random_seed": 5})
+    dec.set_Gate_Structure(c)
+    assert dec.optimizer == "ADAM"
+    x0 = rng.uniform(0, 2 * np.pi, P)
+    xg, xo = x0.copy(), x0.copy()
+    fg_gpu, ng = optim.adam_squander(dec._fg, xg, max_iters=200, seed=8)
+    fg_orc, no = optim.adam_squander(lambda th: O.cost_grad(n, c.gate_records(), th, T), xo, max_iters=200, seed=8)
+    assert ng == no == 200
+    assert abs(fg_gpu - fg_orc) <= 1e-10 * max(1.0, abs(fg_orc))
+    assert np.allclose(xg, xo, atol=1e-9)
+    dec.set_Optimized_Parameters(x0)
+    dec.Start_Decomposition()
+    assert dec.get_Decomposition_Error() <= fg_orc + 1e-9
