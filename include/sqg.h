@@ -72,7 +72,10 @@ const char* sqg_last_error(void);
  * by the caller in order).  Replaces the gate structure a decomposition receives via
  * set_Gate_Structure (squander/decomposition/qgd_N_Qubit_Decompositions_Wrapper.cpp:899)
  * and the gate list of Gates_block (src-cpp/gates/Gates_block.cpp:2500).  qbit_num
- * 1..13.  Copies the gate table to the current device. */
+ * 1..30; the matrix entry points (cost, gradient, application to matrices, combined
+ * unitary, ragged batches) accept up to 13 qubits, the batched decompositions up to 5, the
+ * state-vector application up to 30.  Copies the gate table and the fused state-vector
+ * plan to the current device. */
 int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_circuit** out);
 int sqg_circuit_destroy(sqg_circuit* circuit);
 int sqg_circuit_param_num(const sqg_circuit* circuit);
@@ -157,6 +160,21 @@ int sqg_apply(const sqg_circuit* circuit, const double* theta_dev, int batch, vo
 
 /* In-place right application M <- M C(theta) (cols = 2^qbit_num).  Replaces
  * Gates_block::apply_from_right (src-cpp/gates/Gates_block.cpp:885-935). */
+/* State vectors (cols = 1) of up to 30 qubits: applies the circuit in place to batch
+ * vectors of 2^qbit_num amplitudes (vector b at states_dev + b * state_stride, stride >=
+ * 2^qbit_num).  Replaces Gate::apply_to / Gates_block::apply_to on state-vector inputs
+ * (src-cpp/gates/Gate.cpp:1710-1726, apply_kernel_to_state_vector_input*; driven by
+ * examples/simulation/QC_sim_benchmark.py).  fused != 0 groups consecutive gates whose qubits,
+ * together with the five lowest, number at most 12 into blocks (the role of the reference's
+ * partitioning into fused blocks, squander/partitioning) and applies each block to chunks of
+ * 4096 amplitudes in shared memory: one read and write of the state per block
+ * (sqg_state_block_count); fused == 0 makes one pass per gate.  Circuit handles of more than
+ * 13 qubits are accepted only by this entry point.  Workspace: sqg_state_workspace_bytes. */
+size_t sqg_state_workspace_bytes(const sqg_circuit* circuit, int batch);
+int sqg_state_block_count(const sqg_circuit* circuit);
+int sqg_apply_state(const sqg_circuit* circuit, const double* theta_dev, int batch, void* states_dev,
+                    long long state_stride, int fused, void* workspace_dev, size_t workspace_bytes, void* stream);
+
 int sqg_apply_from_right(const sqg_circuit* circuit, const double* theta_dev, void* mtx_dev, int rows,
                          long long stride, void* workspace_dev, size_t workspace_bytes, void* stream);
 

@@ -120,6 +120,10 @@ def _declare(lib):
     lib.sqg_probe_fp64_tflops.argtypes = [ctypes.POINTER(ctypes.c_double), c_int, vp, c_sz, vp]
     lib.sqg_decompose_workspace_bytes.restype = c_sz
     lib.sqg_decompose_workspace_bytes.argtypes = [vp, c_int, c_int]
+    lib.sqg_state_workspace_bytes.restype = c_sz
+    lib.sqg_state_workspace_bytes.argtypes = [vp, c_int]
+    lib.sqg_state_block_count.argtypes = [vp]
+    lib.sqg_apply_state.argtypes = [vp, vp, c_int, vp, c_ll, c_int, vp, c_sz, vp]
     lib.sqg_decompose_batched_adam.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double,
                                                c_int, ctypes.c_double, c_int, c_int, c_ll, c_int, ctypes.c_uint64, vp]
     lib.sqg_decompose_batched.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double,
@@ -166,6 +170,7 @@ EXPORTED_SYMBOLS = [
     "sqg_cost_grad_checkpoint_workspace_bytes", "sqg_cost_grad", "sqg_cost_grad_noalloc", "sqg_apply_workspace_bytes",
     "sqg_apply",
     "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched", "sqg_decompose_batched_adam",
+    "sqg_state_workspace_bytes", "sqg_state_block_count", "sqg_apply_state",
     "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
     "sqg_mlp_gemm_bf16", "sqg_mlp_to_bf16", "sqg_mlp_relu_backward", "sqg_mlp_col_sum", "sqg_mlp_adam",
     "sqg_mlp_angle_head", "sqg_mlp_features",

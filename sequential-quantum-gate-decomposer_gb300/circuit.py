@@ -169,6 +169,26 @@ class Circuit:
                                               dev.ptr(ws), ws.numel(), dev.stream_ptr(stream)), "sqg_apply")
         return mtx_dev
 
+    def apply_state_device(self, params_dev, states_dev, fused=True, stream=None):
+        """In place psi <- C(params) psi for CUDA complex128 state vectors (2^n,) or a batch
+        (B, 2^n) with params (B, P); up to 30 qubits (sqg_apply_state)."""
+        nc = self.native()
+        B = states_dev.shape[0] if states_dev.dim() == 2 else 1
+        if states_dev.shape[-1] != (1 << self.qbit_num):
+            raise ValueError("Gates_block::apply_to: Wrong input size in Gates_block gate apply.")
+        if not states_dev.is_contiguous():
+            raise ValueError("state must be contiguous")
+        lib = _native.lib()
+        ws = self._ws.get(lib.sqg_state_workspace_bytes(nc.handle, B))
+        _native.check(lib.sqg_apply_state(nc.handle, dev.ptr(params_dev) if params_dev.numel() else None, B,
+                                          dev.ptr(states_dev), states_dev.shape[-1], 1 if fused else 0, dev.ptr(ws),
+                                          ws.numel(), dev.stream_ptr(stream)), "sqg_apply_state")
+        return states_dev
+
+    def state_block_count(self):
+        """Fused passes over a state vector (blocks of the state-vector plan)."""
+        return _native.lib().sqg_state_block_count(self.native().handle)
+
     # ---- SQUANDER-compatible host API (numpy in, numpy out / in place) ---------------
     def get_Matrix(self, parameters_mtx, is_f32=False):
         if is_f32:
@@ -196,6 +216,12 @@ class Circuit:
         if np.asarray(parameters_mtx).dtype != np.float64:
             raise TypeError("parameters must be float64")
         params = self._params_dev(parameters_mtx)
+        if view.shape[1] == 1:
+            # state vector (the reference's state-vector kernels): any register up to 30 qubits
+            psi = dev.to_device_complex(np.ascontiguousarray(view.reshape(-1)))
+            self.apply_state_device(params, psi)
+            view[...] = psi.cpu().numpy().reshape(-1, 1)
+            return
         m = dev.to_device_complex(np.ascontiguousarray(view))
         self.apply_to_device(params, m)
         view[...] = m.cpu().numpy()

@@ -257,8 +257,11 @@ int set_smem(K kernel, size_t bytes) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess && bytes > (size_t)optin) return fail(SQG_ERR_UNSUPPORTED, "tile exceeds shared memory");
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+    const size_t dyn_max = e == cudaSuccess ? (size_t)optin - fa.sharedSizeBytes : 0;  // minus static shared memory
+    if (e == cudaSuccess && bytes > dyn_max) return fail(SQG_ERR_UNSUPPORTED, "tile exceeds shared memory");
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max);
     if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
   }
   return SQG_OK;
@@ -304,12 +307,134 @@ int launch_prep(const sqg_circuit* c, const double* theta, long long theta_strid
   return cuda_status(cudaGetLastError(), "k_prep");
 }
 
-int check_circuit(const sqg_circuit* c) {
+// Matrix entry points hold whole columns in shared memory: qbit_num <= kMatrixQubits.
+constexpr int kMatrixQubits = 13;
+
+int check_circuit(const sqg_circuit* c, int max_n = kMatrixQubits) {
   if (!c) return fail(SQG_ERR_INVALID_ARGUMENT, "null circuit handle");
   int dev = -1;
   cudaGetDevice(&dev);
   if (dev != c->device) return fail(SQG_ERR_INVALID_ARGUMENT, "circuit handle belongs to another device");
+  if (c->n > max_n)
+    return fail(SQG_ERR_UNSUPPORTED, "this entry point supports qbit_num <= " + std::to_string(max_n) +
+                                         " (state vectors up to 30 qubits: sqg_apply_state)");
   return SQG_OK;
+}
+
+// ---- state vectors ---------------------------------------------------------------------
+constexpr int kStateQubits = 30;   // largest register of sqg_apply_state (2^30 amplitudes, 16 GiB)
+constexpr int kStateK = 12;        // qubits per chunk: 4096 amplitudes, 64 KB of shared memory
+constexpr int kStateLow = 5;       // the lowest qubits belong to every chunk (512-byte coalesced runs)
+constexpr int kStateThreads = 256;
+
+// Groups the gates into blocks: a block grows while the qubits it touches, together with the
+// lowest kStateLow ones, number at most K; each block is one pass over the state.  Fills the
+// chunk with further qubits (lowest first), maps every gate of the block to chunk-local qubit
+// positions and tabulates the global offsets of the chunk's high local bits and the qubits
+// that number the chunks.
+int build_state_plan(sqg_circuit* c) {
+  const int n = c->n, K = std::min(n, kStateK), low = std::min(K, kStateLow);
+  c->sK = K;
+  std::vector<Gate> lg(c->h_gates);
+  std::vector<int> hitab, inact;
+  std::vector<int> inA(n, 0);
+  auto close_block = [&](int g0, int g1) {
+    std::vector<int> A;
+    for (int q = 0; q < n; q++)
+      if (q < low || inA[q]) A.push_back(q);
+    for (int q = 0; q < n && (int)A.size() < K; q++)
+      if (!(q < low || inA[q])) {
+        A.push_back(q);
+        inA[q] = 1;
+      }
+    std::sort(A.begin(), A.end());
+    std::vector<int> loc(n, -1);
+    for (int j = 0; j < (int)A.size(); j++) loc[A[j]] = j;
+    for (int g = g0; g < g1; g++) {
+      lg[g].target = loc[c->h_gates[g].target];
+      if (gate_controlled(c->h_gates[g].type)) lg[g].control = loc[c->h_gates[g].control];
+    }
+    const int hb = K - low;
+    for (int h = 0; h < 128; h++) {
+      int off = 0;
+      if (h < (1 << hb))
+        for (int j = 0; j < hb; j++)
+          if ((h >> j) & 1) off |= 1 << A[low + j];
+      hitab.push_back(off);
+    }
+    int k = 0;
+    for (int q = 0; q < n; q++)
+      if (loc[q] < 0) {
+        inact.push_back(q);
+        k++;
+      }
+    for (; k < 32; k++) inact.push_back(0);
+    c->sblocks.push_back({g0, g1});
+    std::fill(inA.begin(), inA.end(), 0);
+  };
+  int g0 = 0, used = 0;
+  for (int g = 0; g < c->L; g++) {
+    const Gate& gt = c->h_gates[g];
+    int add = 0;
+    int qs[2] = {gt.target, gate_controlled(gt.type) ? gt.control : -1};
+    for (int q : qs)
+      if (q >= low && !inA[q]) add++;
+    if (low + used + add > K) {
+      close_block(g0, g);
+      g0 = g;
+      used = 0;
+    }
+    for (int q : qs)
+      if (q >= low && !inA[q]) {
+        inA[q] = 1;
+        used++;
+      }
+  }
+  if (c->L > 0) close_block(g0, c->L);
+  if (c->L == 0) return SQG_OK;
+  cudaError_t e = cudaMalloc(&c->d_lgates, sizeof(Gate) * c->L);
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_lgates, lg.data(), sizeof(Gate) * c->L, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_hitab, sizeof(int) * hitab.size());
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_hitab, hitab.data(), sizeof(int) * hitab.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_inact, sizeof(int) * inact.size());
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_inact, inact.data(), sizeof(int) * inact.size(), cudaMemcpyHostToDevice);
+  return cuda_status(e, "state plan");
+}
+
+// One block of gates applied to every chunk of 2^K amplitudes of a state vector.  The
+// chunk's low local bits are the state's lowest qubits (a warp loads 32 consecutive
+// amplitudes), its high local bits are the block's other qubits (offsets from hitab), and the
+// remaining qubits number the chunks (inact).  One read and one write of the state per block.
+struct StateArgs {
+  double2* states;
+  long long stride;
+  int n, K, low, g0, g1, L;
+  const Gate* lgates;
+  const GateMat* gm;
+  const int* hitab;
+  const int* inact;
+};
+
+__global__ void __launch_bounds__(kStateThreads) k_state_block(StateArgs a) {
+  extern __shared__ double2 sv[];
+  __shared__ int hit[128];
+  const int b = blockIdx.y;
+  const int KK = 1 << a.K, hb = a.K - a.low, lowmask = (1 << a.low) - 1;
+  for (int h = threadIdx.x; h < (1 << hb); h += blockDim.x) hit[h] = a.hitab[h];
+  long long cbase = 0;
+  for (int j = 0; j < a.n - a.K; j++)
+    if ((blockIdx.x >> j) & 1u) cbase |= 1LL << a.inact[j];
+  double2* base = a.states + (long long)b * a.stride + cbase;
+  __syncthreads();
+  for (int l = threadIdx.x; l < KK; l += blockDim.x) sv[l] = base[(l & lowmask) + hit[l >> a.low]];
+  __syncthreads();
+  const GateMat* gmb = a.gm + (long long)b * a.L;
+  for (int g = a.g0; g < a.g1; g++) {
+    const Gate gt = a.lgates[g];
+    tile_apply(sv, KK, a.K, 1, gt, make_op(gt.type, gmb[g], ORIENT_FWD));
+    __syncthreads();
+  }
+  for (int l = threadIdx.x; l < KK; l += blockDim.x) base[(l & lowmask) + hit[l >> a.low]] = sv[l];
 }
 
 }  // namespace
@@ -336,7 +461,7 @@ const char* sqg_last_error(void) { return g_last_error.c_str(); }
 int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_circuit** out) {
   if (!out) return fail(SQG_ERR_INVALID_ARGUMENT, "null output handle");
   *out = nullptr;
-  if (qbit_num < 1 || qbit_num > 13) return fail(SQG_ERR_UNSUPPORTED, "qbit_num must be in 1..13");
+  if (qbit_num < 1 || qbit_num > kStateQubits) return fail(SQG_ERR_UNSUPPORTED, "qbit_num must be in 1..30");
   if (gate_num < 0 || (gate_num > 0 && !gates)) return fail(SQG_ERR_INVALID_ARGUMENT, "bad gate list");
   auto* c = new sqg_circuit();
   c->n = qbit_num;
@@ -378,10 +503,14 @@ int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_ci
     if (e == cudaSuccess) e = cudaMemcpy(c->d_gates, c->h_gates.data(), sizeof(Gate) * gate_num, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
       int st = cuda_status(e, "sqg_circuit_create");
-      cudaFree(c->d_gates);
-      delete c;
+      sqg_circuit_destroy(c);
       return st;
     }
+  }
+  int st = build_state_plan(c);
+  if (st) {
+    sqg_circuit_destroy(c);
+    return st;
   }
   *out = c;
   return SQG_OK;
@@ -390,6 +519,9 @@ int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_ci
 int sqg_circuit_destroy(sqg_circuit* c) {
   if (!c) return SQG_OK;
   if (c->d_gates) cudaFree(c->d_gates);
+  if (c->d_lgates) cudaFree(c->d_lgates);
+  if (c->d_hitab) cudaFree(c->d_hitab);
+  if (c->d_inact) cudaFree(c->d_inact);
   delete c;
   return SQG_OK;
 }
@@ -644,6 +776,63 @@ int sqg_combined_unitary(const sqg_circuit* c, const double* theta, const void* 
     created += np;
   }
   return cuda_status(cudaGetLastError(), "sqg_combined_unitary");
+}
+
+
+size_t sqg_state_workspace_bytes(const sqg_circuit* c, int batch) {
+  if (!c || batch <= 0) return 0;
+  return prep_layout(c, batch, 0).end;
+}
+
+int sqg_state_block_count(const sqg_circuit* c) { return c ? (int)c->sblocks.size() : -1; }
+
+int sqg_apply_state(const sqg_circuit* c, const double* theta, int B, void* states, long long stride, int fused,
+                    void* workspace, size_t ws_bytes, void* stream) {
+  int st = check_circuit(c, kStateQubits);
+  if (st) return st;
+  if (B <= 0 || B > 65535 || !states || stride < (long long)c->N)
+    return fail(SQG_ERR_INVALID_ARGUMENT, "bad state arguments (batch 1..65535, stride >= 2^qbit_num)");
+  if (c->P > 0 && !theta) return fail(SQG_ERR_INVALID_ARGUMENT, "null parameter array");
+  PrepLayout l = prep_layout(c, B, 0);
+  if (!workspace || ws_bytes < l.end) return fail(SQG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(l.end));
+  if (c->L == 0) return SQG_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* ws = (char*)workspace;
+  GateMat* gm = (GateMat*)(ws + l.gm_off);
+  double2* sc = (double2*)(ws + l.sc_off);
+  if ((st = launch_prep(c, theta, c->P, B, gm, sc, s))) return st;
+  if (fused) {
+    const size_t smem = sizeof(double2) << c->sK;
+    if ((st = set_smem(k_state_block, smem))) return st;
+    StateArgs a;
+    a.states = (double2*)states;
+    a.stride = stride;
+    a.n = c->n;
+    a.K = c->sK;
+    a.low = std::min(c->sK, kStateLow);
+    a.L = c->L;
+    a.lgates = c->d_lgates;
+    a.gm = gm;
+    for (size_t k = 0; k < c->sblocks.size(); k++) {
+      a.g0 = c->sblocks[k].g0;
+      a.g1 = c->sblocks[k].g1;
+      a.hitab = c->d_hitab + 128 * k;
+      a.inact = c->d_inact + 32 * k;
+      k_state_block<<<dim3(1u << (c->n - c->sK), B), kStateThreads, smem, s>>>(a);
+    }
+    return cuda_status(cudaGetLastError(), "k_state_block");
+  }
+  // unfused: one pass over the state per gate
+  for (int b = 0; b < B; b++) {
+    double2* base = (double2*)states + (long long)b * stride;
+    for (int g = 0; g < c->L; g++) {
+      const Gate& gt = c->h_gates[g];
+      long long items = 1LL << (gate_controlled(gt.type) ? c->n - 2 : c->n - 1);
+      k_gate_hbm<<<dim3(hbm_blocks(items), 1), 256, 0, s>>>(base, 0, 1, 1, c->n, gt, gm + (long long)b * c->L + g,
+                                                          sc + (long long)b * c->P, -1, 1);
+    }
+  }
+  return cuda_status(cudaGetLastError(), "k_gate_hbm");
 }
 
 }  // extern "C"

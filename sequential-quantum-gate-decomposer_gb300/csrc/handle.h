@@ -6,11 +6,25 @@
 
 #include "gates.cuh"
 
+// Fused state-vector passes (sqg_apply_state): consecutive gates whose qubits, together with
+// the lowest ones, fit one chunk of 2^K amplitudes form a block applied in shared memory.
+struct sqg_state_block {
+  int g0, g1;  // gates [g0, g1)
+};
+
 struct sqg_circuit {
   int n = 0, N = 0, L = 0, P = 0;
   int device = 0;
   sqg::Gate* d_gates = nullptr;
   std::vector<sqg::Gate> h_gates;
+  // state-vector plan: chunk qubits K, blocks, gate records with chunk-local qubit positions,
+  // per block the global offsets of the chunk's high local bits (2^(K - low) ints, padded to
+  // 128) and the qubits that number the chunks (padded to 32)
+  int sK = 0;
+  std::vector<sqg_state_block> sblocks;
+  sqg::Gate* d_lgates = nullptr;
+  int* d_hitab = nullptr;
+  int* d_inact = nullptr;
 };
 
 namespace sqg {

@@ -204,6 +204,10 @@ int sqg_ragged_create(const sqg_circuit* const* circuits, const int* cols, int c
       free_batch(r);
       return set_error(SQG_ERR_INVALID_ARGUMENT, "instance " + std::to_string(i) + ": bad circuit or target width");
     }
+    if (c->n > 13) {
+      free_batch(r);
+      return set_error(SQG_ERR_UNSUPPORTED, "ragged batches hold whole columns on chip: qbit_num <= 13");
+    }
     if (with_grad && c->n > 12) {
       free_batch(r);
       return set_error(SQG_ERR_UNSUPPORTED, "gradient supports qbit_num <= 12");

@@ -70,6 +70,46 @@ def random_gate_circuit(n, gates, rng):
     return c
 
 
+def all_gates_circuit(n, gates, rng):
+    """`gates` gates drawn uniformly from all seven supported kinds on uniform qubits."""
+    c = Circuit(n)
+    for _ in range(gates):
+        kind = int(rng.integers(7))
+        t = int(rng.integers(n))
+        ctl = int(rng.integers(n - 1)) if n > 1 else 0
+        ctl = ctl + 1 if ctl >= t else ctl
+        if kind == 0 or n == 1:
+            c.add_U3(t)
+        elif kind == 1:
+            c.add_RX(t)
+        elif kind == 2:
+            c.add_RY(t)
+        elif kind == 3:
+            c.add_RZ(t)
+        elif kind == 4:
+            c.add_CNOT(t, ctl)
+        elif kind == 5:
+            c.add_CZ(t, ctl)
+        else:
+            c.add_CRY(t, ctl)
+    return c
+
+
+def qc_sim_circuit(n, levels=4):
+    """The circuit of SQUANDER's state-vector simulation benchmark
+    (examples/simulation/QC_sim_benchmark.py): `levels` sweeps over all qubit pairs
+    c < t of [U3(t), U3(c), CRY(target t, control c)], then a U3 on qubit 0."""
+    c = Circuit(n)
+    for _ in range(levels):
+        for ctl in range(n - 1):
+            for t in range(ctl + 1, n):
+                c.add_U3(t)
+                c.add_U3(ctl)
+                c.add_CRY(t, ctl)
+    c.add_U3(0)
+    return c
+
+
 def _one_qubit(t, p, ps):
     if t == 7:  # U3 (theta/2, phi, lambda)
         c, s = np.cos(p[ps]), np.sin(p[ps])

@@ -1,0 +1,84 @@
+"""State-vector application (sqg_apply_state, up to 30 qubits) against the oracle: fused
+blocks and one pass per gate, batches, the drop-in Circuit.apply_to on 1-D states, and at
+sizes the oracle cannot reach, size-independent properties (norm, fused == unfused)."""
+import importlib
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def wl():
+    return importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+
+
+def random_state(n, rng, batch=None):
+    shape = (1 << n,) if batch is None else (batch, 1 << n)
+    v = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    return v / np.linalg.norm(v, axis=-1, keepdims=True)
+
+
+@pytest.mark.parametrize("n,gates", [(3, 40), (12, 300), (14, 400), (16, 300)])
+def test_state_matches_oracle(sqg, wl, n, gates):
+    rng = np.random.default_rng(100 + n)
+    c = wl.all_gates_circuit(n, gates, rng)
+    P = c.get_Parameter_Num()
+    p = rng.uniform(0, 2 * np.pi, P)
+    psi = random_state(n, rng)
+    ref = O.apply_to(n, c.gate_records(), p, psi.reshape(-1, 1).copy()).reshape(-1)
+    th = torch.from_numpy(p).cuda()
+    for fused in (True, False):
+        d = torch.from_numpy(psi.copy()).cuda()
+        c.apply_state_device(th, d, fused=fused)
+        torch.cuda.synchronize()
+        assert float(np.abs(d.cpu().numpy() - ref).max()) < 1e-12, fused
+    assert 1 <= c.state_block_count() <= c.get_Gate_Num()
+
+
+def test_state_batch_and_dropin_apply_to(sqg, wl):
+    n, B = 15, 3
+    rng = np.random.default_rng(7)
+    c = wl.all_gates_circuit(n, 200, rng)
+    P = c.get_Parameter_Num()
+    p = rng.uniform(0, 2 * np.pi, (B, P))
+    psi = random_state(n, rng, B)
+    d = torch.from_numpy(psi.copy()).cuda()
+    c.apply_state_device(torch.from_numpy(p).cuda(), d)
+    torch.cuda.synchronize()
+    got = d.cpu().numpy()
+    for b in range(B):
+        ref = O.apply_to(n, c.gate_records(), p[b], psi[b].reshape(-1, 1).copy()).reshape(-1)
+        assert float(np.abs(got[b] - ref).max()) < 1e-12
+    # Circuit.apply_to on a 1-D state works in place, as the reference's (qgd_Circuit.py:546)
+    v = psi[0].copy()
+    c.apply_to(p[0], v)
+    assert float(np.abs(v - got[0]).max()) < 1e-13
+
+
+def test_matrix_entry_points_reject_large_registers(sqg, wl):
+    c = wl.all_gates_circuit(14, 10, np.random.default_rng(1))
+    with pytest.raises(Exception):
+        c.get_Matrix(np.zeros(c.get_Parameter_Num()))
+
+
+@pytest.mark.parametrize("n", [20, 24])
+def test_qc_sim_circuit_large_state(sqg, wl, n):
+    """The reference's simulation-benchmark circuit at sizes beyond the oracle: the norm is
+    kept to 1e-12 and fused blocks give the result of one pass per gate."""
+    rng = np.random.default_rng(n)
+    c = wl.qc_sim_circuit(n, levels=4 if n == 20 else 1)
+    th = torch.from_numpy(rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())).cuda()
+    psi = torch.from_numpy(random_state(n, rng)).cuda()
+    a = psi.clone()
+    b = psi.clone()
+    c.apply_state_device(th, a, fused=True)
+    c.apply_state_device(th, b, fused=False)
+    torch.cuda.synchronize()
+    assert abs(float(torch.linalg.vector_norm(a)) - 1.0) < 1e-12
+    assert float((a - b).abs().max()) < 1e-12
+    assert c.state_block_count() < c.get_Gate_Num() / 4
