@@ -304,6 +304,7 @@ def bench_ours(args):
         line["cost_grad_uneven"] = bench_ragged(sqg, wl, torch)
         line["cost_grad_n10"] = bench_cost_grad_n10(sqg, wl, torch)
         line["decompose_n4_single"] = bench_single_n4(sqg, wl, torch)
+        line["state_vector_n24"] = bench_state_vector(sqg, wl, torch)
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(sqg, wl, ansatz, targets, P, budget_s=args.cpu_seconds)
     return line
@@ -485,6 +486,54 @@ def bench_cost_grad_n10(sqg, wl, torch):
         ops = fp64_ops_per_eval(c.gate_records(), 1024, 1024) * 64
         out["checkpoint_%d" % ck] = {"seconds": t, "evals_per_s": 64 / t, "fp64_tflops": 2.0 * ops / t / 1e12}
     return out
+
+
+def state_flops(circuit_records, n):
+    """Algorithmic flops of one application to a 2^n state vector: 16 flop per touched
+    complex element (two complex multiply-adds), CRY on the control = 1 half; CNOT and CZ
+    are exchanges and sign flips."""
+    f = 0
+    for t, tg, c, ps in circuit_records:
+        if t in (7, 8, 9, 10):
+            f += 16 * (1 << n)
+        elif t == 14:
+            f += 16 * (1 << (n - 1))
+    return f
+
+
+def bench_state_vector(sqg, wl, torch):
+    """The state-vector simulation benchmark circuit of SQUANDER
+    (examples/simulation/QC_sim_benchmark.py) at n = 24: 4 sweeps of [U3, U3, CRY] over all
+    qubit pairs (3313 gates) applied to a random normalised state (256 MB), fused blocks vs one
+    pass per gate."""
+    hbm, src = peaks()
+    n = 24
+    rng = np.random.default_rng(24)
+    c = wl.qc_sim_circuit(n, levels=4)
+    th = torch.from_numpy(rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())).cuda()
+    v = torch.randn(1 << n, dtype=torch.complex128, device="cuda")
+    v /= torch.linalg.vector_norm(v)
+    flops = state_flops(c.gate_records(), n)
+    res = {"config": "n=24 state vector (256 MB), SQUANDER QC_sim_benchmark circuit, 4 levels, %d gates"
+                     % c.get_Gate_Num(), "blocks": c.state_block_count()}
+    for fused in (True, False):
+        c.apply_state_device(th, v, fused=fused)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c.apply_state_device(th, v, fused=fused)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        passes = c.state_block_count() if fused else c.get_Gate_Num()
+        hbm_gbs = passes * 2 * 16 * (1 << n) / t / 1e9
+        res["fused" if fused else "unfused"] = {
+            "seconds": t, "fp64_tflops": flops / t / 1e12, "fp64_frac": flops / t / 1e12 / FP64_PEAK_TFLOPS,
+            "hbm_pass_GBps": hbm_gbs, "hbm_frac": hbm_gbs / hbm}
+    res["norm_after"] = float(torch.linalg.vector_norm(v))
+    res["peak_hbm_GBps"] = hbm
+    res["peak_source"] = src
+    return res
 
 
 def cpu_baseline(sqg, wl, ansatz, targets, P, budget_s=20.0):
