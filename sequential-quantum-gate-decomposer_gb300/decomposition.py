@@ -96,8 +96,14 @@ class N_Qubit_Decomposition_custom:
             print("Wrong optimizer: %s. Using default: BFGS" % optimizer)
             name = "BFGS"
         self.optimizer = name
-        # Optimization_Interface::set_optimizer defaults (Optimization_Interface.cpp:1620-1697)
-        self.max_inner_iterations = 10000 if name == "BFGS" else 100000
+        # Optimization_Interface::set_optimizer (Optimization_Interface.cpp:1619-1670): BFGS runs
+        # 10000 evaluations per run and outer iterations until the tolerance; ADAM 100000
+        # evaluations in one outer iteration with up to 100 randomisations.  The constructor
+        # then sets 4 (BFGS) or 1 (ADAM) outer iterations, N_Qubit_Decomposition_custom.cpp:59-76.
+        if name == "BFGS":
+            self.max_inner_iterations, self.max_outer_iterations, self.random_shift_count_max = 10000, 100000000, 1
+        else:
+            self.max_inner_iterations, self.max_outer_iterations, self.random_shift_count_max = 100000, 1, 100
         return 0
 
     def set_Optimization_Tolerance(self, tolerance):
@@ -244,7 +250,7 @@ class N_Qubit_Decomposition_custom:
                 tol_a = float(cfg.get("optimization_tolerance_adam", tol))
                 x = guess.copy()
                 f, calls = adam_squander(self._fg, x, max_inner, tol_a, eta, adaptive,
-                                         int(cfg.get("random_shift_count_max", 100)), thr,
+                                         int(cfg.get("random_shift_count_max", self.random_shift_count_max)), thr,
                                          seed=int(self.rng.integers(1 << 62)), current_minimum=best_f)
                 self.num_iters += calls
                 if f < best_f:
