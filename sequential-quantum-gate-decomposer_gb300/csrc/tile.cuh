@@ -120,16 +120,32 @@ __device__ __forceinline__ double2 tile_trace(const double2* s, int N, int tc, i
 // FP64 pipe is charged per warp instruction whatever the number of active lanes.
 // redd: kTileMaxWarps * 8 doubles, tot: 8 doubles.  restore(g) is called at the start of
 // each reverse step and may overwrite psi (checkpoints); it must contain its own barriers.
+// stage_gates / stage_mats (kStage entries each, or null): shared-memory staging of the
+// gate records and matrices when gates / gm are in global memory.
+constexpr int kStage = 32;
+
 template <class Sink, class Restore>
 __device__ __forceinline__ void adjoint_sweep(double2* psi, double2* lam, int N, int logN, int tc, const Gate* gates,
                                               const GateMat* gm, const double2* sc, int L, double* redd, double* tot,
-                                              Sink sink, Restore restore) {
+                                              Sink sink, Restore restore, Gate* stage_gates = nullptr,
+                                              GateMat* stage_mats = nullptr) {
   const int nw = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool staged = stage_gates != nullptr;
   for (int g = L - 1; g >= 0; g--) {
+    const int j = (L - 1 - g) % kStage;  // position of gate g in its staged chunk
+    if (staged && j == 0) {
+      __syncthreads();
+      const int kn = min(kStage, g + 1);
+      if ((int)threadIdx.x < kn) {
+        stage_gates[threadIdx.x] = gates[g - threadIdx.x];
+        stage_mats[threadIdx.x] = gm[g - threadIdx.x];
+      }
+      __syncthreads();
+    }
     restore(g);
-    Gate gt = gates[g];
-    PairOp op = make_op(gt.type, gm[g], ORIENT_ADJ);
+    Gate gt = staged ? stage_gates[j] : gates[g];
+    PairOp op = make_op(gt.type, staged ? stage_mats[j] : gm[g], ORIENT_ADJ);
     const int np = gate_param_num(gt.type);
     if (np == 0) {
       tile_apply(psi, N, logN, tc, gt, op);

@@ -63,25 +63,42 @@ __device__ __forceinline__ void store_tile(const double2* s, const TileArgs& a, 
   }
 }
 
+// Gate records and 2x2 matrices are staged in shared memory kGateChunk at a time, so each
+// CTA reads them from global memory once instead of once per warp and gate.
+constexpr int kGateChunk = kStage;
+constexpr size_t kGateStageBytes = kGateChunk * (sizeof(Gate) + sizeof(GateMat));
+
 // Forward (or right) application of the whole circuit to one tile; optionally writes
 // the tile back and/or the traced diagonal partial.
 template <bool WRITE_BACK, bool TRACE>
 __device__ __forceinline__ void tile_forward_body(const TileArgs& a, int b, int tile, double2* smem) {
   double2* s = smem;
   double2* red = smem + (size_t)a.TC * a.N;
+  GateMat* gst = reinterpret_cast<GateMat*>(red + kTileMaxWarps);  // [kGateChunk]
+  Gate* gts = reinterpret_cast<Gate*>(gst + kGateChunk);            // [kGateChunk]
   const int v0 = tile * a.TC;
   const int tc = min(a.TC, a.cols - v0);
   const int logN = a.n;
   load_tile(s, a, b, v0, tc);
-  __syncthreads();
   const GateMat* gm = a.gm + (long long)b * a.L;
-  for (int k = 0; k < a.L; k++) {
-    int g = a.reverse_order ? a.L - 1 - k : k;
-    Gate gt = a.gates[g];
-    PairOp op = make_op(gt.type, gm[g], a.orient);
-    tile_apply(s, a.N, logN, tc, gt, op);
+  for (int k0 = 0; k0 < a.L; k0 += kGateChunk) {
+    const int kn = min(kGateChunk, a.L - k0);
+    __syncthreads();  // the previous chunk's records are no longer read
+    if (threadIdx.x < kn) {
+      const int k = k0 + threadIdx.x;
+      const int g = a.reverse_order ? a.L - 1 - k : k;
+      gts[threadIdx.x] = a.gates[g];
+      gst[threadIdx.x] = gm[g];
+    }
     __syncthreads();
+    for (int j = 0; j < kn; j++) {
+      const Gate gt = gts[j];
+      PairOp op = make_op(gt.type, gst[j], a.orient);
+      tile_apply(s, a.N, logN, tc, gt, op);
+      __syncthreads();
+    }
   }
+  __syncthreads();
   if (TRACE) {
     double2 t = tile_trace(s, a.N, tc, v0, a.trace_offset, reinterpret_cast<double*>(red));
     if (threadIdx.x == 0) a.ws_tr[(long long)b * a.tiles + tile] = t;
@@ -97,6 +114,8 @@ __device__ __forceinline__ void tile_adjoint_body(const TileArgs& a, int b, int 
   double* redd = reinterpret_cast<double*>(lam + (size_t)a.TC * N);  // [kTileMaxWarps][8]
   double* tot = redd + kTileMaxWarps * 8;                             // [8]
   double* scratch = tot + 8;                                          // [kTileMaxWarps]
+  GateMat* gst = reinterpret_cast<GateMat*>(scratch + kTileMaxWarps);  // [kGateChunk]
+  Gate* gts = reinterpret_cast<Gate*>(gst + kGateChunk);              // [kGateChunk]
   const int v0 = tile * a.TC;
   const int tc = min(a.TC, a.cols - v0);
   const size_t tile_elems = (size_t)a.TC * N;
@@ -113,8 +132,17 @@ __device__ __forceinline__ void tile_adjoint_body(const TileArgs& a, int b, int 
   const double2* scb = a.sc + (long long)b * a.P;
   // forward sweep, storing psi after every ckpt_interval-th gate
   for (int g = 0; g < a.L; g++) {
-    Gate gt = a.gates[g];
-    PairOp op = make_op(gt.type, gm[g], ORIENT_FWD);
+    const int j = g % kGateChunk;
+    if (j == 0) {
+      __syncthreads();
+      if ((int)threadIdx.x < min(kGateChunk, a.L - g)) {
+        gts[threadIdx.x] = a.gates[g + threadIdx.x];
+        gst[threadIdx.x] = gm[g + threadIdx.x];
+      }
+      __syncthreads();
+    }
+    Gate gt = gts[j];
+    PairOp op = make_op(gt.type, gst[j], ORIENT_FWD);
     tile_apply(psi, N, logN, tc, gt, op);
     __syncthreads();
     if (ck && (g + 1) % a.ckpt_interval == 0 && (g + 1) / a.ckpt_interval <= a.nck) {
@@ -139,14 +167,15 @@ __device__ __forceinline__ void tile_adjoint_body(const TileArgs& a, int b, int 
       __syncthreads();
     }
   };
-  adjoint_sweep(psi, lam, N, logN, tc, a.gates, gm, scb, a.L, redd, tot, sink, restore);
+  adjoint_sweep(psi, lam, N, logN, tc, a.gates, gm, scb, a.L, redd, tot, sink, restore, gts, gst);
 }
 
 
 // Shared memory bytes of one work item: tiles plus reduction scratch.
 __host__ __device__ inline size_t tile_smem_bytes(int TC, int N, bool grad) {
   size_t per = (size_t)N * sizeof(double2) * (grad ? 2 : 1);
-  size_t extra = grad ? (kTileMaxWarps * 8 + 8 + kTileMaxWarps) * sizeof(double) : kTileMaxWarps * sizeof(double2);
+  size_t extra = grad ? (kTileMaxWarps * 8 + 8 + kTileMaxWarps) * sizeof(double) + kGateStageBytes
+                      : kTileMaxWarps * sizeof(double2) + kGateStageBytes;
   return per * TC + extra;
 }
 
