@@ -179,12 +179,20 @@ __global__ void k_gate_hbm(double2* __restrict__ mtx, long long bstride, long lo
   } else {
     op = make_op(gt.type, *gmp, ORIENT_FWD);
   }
+  // items < 2^31 (at most 2^29 pairs of a 30-qubit state, 2^12 x 2^13 pairs of a matrix);
+  // a power-of-two column count splits an item with a shift instead of a division
+  const int logc = (__popc(cols) == 1) ? __ffs(cols) - 1 : -1;
   for (int b = blockIdx.y; b < nmat; b += gridDim.y) {
     double2* base = mtx + (long long)b * bstride;
-    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items;
-         it += (long long)gridDim.x * blockDim.x) {
-      int p = (int)(it / cols);
-      int c = (int)(it - (long long)p * cols);
+    for (unsigned it = blockIdx.x * blockDim.x + threadIdx.x; it < (unsigned)items; it += gridDim.x * blockDim.x) {
+      int p, c;
+      if (logc >= 0) {
+        p = (int)(it >> logc);
+        c = (int)(it & (unsigned)(cols - 1));
+      } else {
+        p = (int)(it / (unsigned)cols);
+        c = (int)(it - (unsigned)p * (unsigned)cols);
+      }
       int i;
       bool active = true;
       if (!deriv) {
