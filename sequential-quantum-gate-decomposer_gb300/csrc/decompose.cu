@@ -407,10 +407,16 @@ __device__ double dec_eval_cyclic2(const DecArgs& a, const Sh& sh, const double*
   return dec_finish(a, sh, make_double2(sh.redd[0], sh.redd[1]), gv);
 }
 
-// Cost and gradient of parameter vector xv (smem) for instance b; gradient into gv.
+// Cost and gradient of parameter vector xv (smem) for instance b; gradient into gv.  FORM
+// (a template parameter, so that each kernel carries the code of one form only):
+// kFormSweep state sweeps, kFormCyclic environment matrix on all warps, kFormTwoChains the
+// two-warp environment matrix.
+enum { kFormSweep = 0, kFormCyclic = 1, kFormTwoChains = 2 };
+
+template <int FORM>
 __device__ double dec_eval(const DecArgs& a, const Sh& sh, const double* xv, double* gv, int b) {
-  if (a.chains == 2) return dec_eval_cyclic2(a, sh, xv, gv);
-  if (a.cyclic) return dec_eval_cyclic(a, sh, xv, gv, b);
+  if constexpr (FORM == kFormTwoChains) return dec_eval_cyclic2(a, sh, xv, gv);
+  if constexpr (FORM == kFormCyclic) return dec_eval_cyclic(a, sh, xv, gv, b);
   const int N = a.N, cols = a.cols, off = a.trace_offset;
   dec_build(a, sh, xv);
   const double2* T = sh.tgt;
@@ -675,13 +681,14 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
 // evaluation budget a.max_calls applies to this run (a new BFGS_Powell with its own call
 // count per restart, optimization_engines/BFGS.cpp:121-125); calls and iters accumulate
 // over the runs of the decomposition.
+template <int FORM>
 __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, int& iters) {
   int run = 0;
   const int P = a.P;
   double* Z = sh.Z;
   for (int i = threadIdx.x; i < P * P; i += blockDim.x) Z[i] = (i % (P + 1)) == 0 ? 1.0 : 0.0;
   double norm_Z = -1.0;
-  double f = dec_eval(a, sh, sh.x, sh.g, b);
+  double f = dec_eval<FORM>(a, sh, sh.x, sh.g, b);
   calls++;
   run++;
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -730,7 +737,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
     for (int it = 0; it < 50; it++) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.x0[i] + step * sh.d[i];
       __syncthreads();
-      f = dec_eval(a, sh, sh.x, sh.g, b);
+      f = dec_eval<FORM>(a, sh, sh.x, sh.g, b);
       calls++;
       run++;
       if (a.early_stop && f < a.tol) return f;
@@ -797,6 +804,7 @@ __device__ __forceinline__ double splitmix_u01(unsigned long long& s) {
 // target's splitmix64 stream.  Adam's bias-correction powers advance once per parameter in
 // parameter order, as in the reference; pw1/pw2 hold beta^(i + 1).  Starts from sh.x, leaves
 // the best point in sh.bestx and returns the minimum.
+template <int FORM>
 __device__ double dec_adam(const DecArgs& a, const Sh& sh, int b, int& calls, int& shifts, double cur_min,
                            unsigned long long& rng, double* f0_vec, int* dec_vec) {
   const int P = a.P;
@@ -829,7 +837,7 @@ __device__ double dec_adam(const DecArgs& a, const Sh& sh, int b, int& calls, in
   long long sub_iter = 0;
   int status = 0, shift_cnt = 0;  // random_shift_count of this engine call
   for (int it = 0; it < a.max_calls; it++) {
-    const double f0 = dec_eval(a, sh, xt, g, b);
+    const double f0 = dec_eval<FORM>(a, sh, xt, g, b);
     calls++;
     if (sub_iter == 1) {
       hold = f0;
@@ -924,7 +932,7 @@ __device__ double dec_adam(const DecArgs& a, const Sh& sh, int b, int& calls, in
 // At most 80 registers (6 CTAs of 128 threads per SM): the evaluation keeps only one warp
 // per CTA busy at n = 3, so resident CTAs are what hides FP64 and shared-memory latency
 // (measured 7470 vs 7103 decompositions/s with the unconstrained 126 registers).
-template <int OPT>
+template <int OPT, int FORM>
 __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   extern __shared__ double2 smem2[];
   const int b = blockIdx.x;
@@ -985,7 +993,7 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     for (int outer = 0; outer < a.max_outer; outer++) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.guess[i];
       __syncthreads();
-      cur_min = dec_adam(a, sh, b, calls, iters, cur_min, rng, f0_vec, dec_vec);
+      cur_min = dec_adam<FORM>(a, sh, b, calls, iters, cur_min, rng, f0_vec, dec_vec);
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = sh.bestx[i];
       __syncthreads();
       if (fabs(cur_min) < a.tol) break;
@@ -998,7 +1006,7 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     for (int loop = 0; loop < a.loops; loop++) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.guess[i];
       __syncthreads();
-      double f = dec_bfgs(a, sh, b, calls, iters);
+      double f = dec_bfgs<FORM>(a, sh, b, calls, iters);
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = sh.x[i];
       __syncthreads();
       if (f < best) {
@@ -1097,21 +1105,29 @@ int two_chain_split(const sqg_circuit& c) {
 }
 
 // Kernel attributes and launch shared by the BFGS and ADAM entry points.
-template <int OPT>
-int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
+template <int OPT, int FORM>
+int dec_launch_form(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e == cudaSuccess && smem > (size_t)optin)
     return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
   // raised to the device maximum, never lowered: the attribute is shared by all callers
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_decompose<OPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
   // one thread per parameter for the vector and Z-matrix work, at least two warps
   const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
-  k_decompose<OPT><<<batch, threads, smem, (cudaStream_t)stream>>>(a);
+  k_decompose<OPT, FORM><<<batch, threads, smem, (cudaStream_t)stream>>>(a);
   e = cudaGetLastError();
   return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
+}
+
+template <int OPT>
+int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
+  if (a.chains == 2) return dec_launch_form<OPT, kFormTwoChains>(c, a, batch, smem, stream);
+  if (a.cyclic) return dec_launch_form<OPT, kFormCyclic>(c, a, batch, smem, stream);
+  return dec_launch_form<OPT, kFormSweep>(c, a, batch, smem, stream);
 }
 
 // Evaluation form of the decomposition kernels for this circuit and target width.
