@@ -54,6 +54,7 @@ struct DecArgs {
   // ADAM engine (k_decompose<kAdam>)
   double eta;
   int adaptive_eta, shift_max;
+  double inv_cols;  // 1 / cols (exact for powers of two)
   long long rand_thr;
 };
 
@@ -123,12 +124,12 @@ __device__ void dec_build(const DecArgs& a, const Sh& sh, const double* xv) {
 __device__ double dec_finish(const DecArgs& a, const Sh& sh, double2 tr, double* gv) {
   const double* Rb = sh.R;
   double f;
-  const double dc = a.cols, inv_dc = 1.0 / dc;
+  const double dc = a.cols, inv_dc = a.inv_cols;
   // x / cols and x * (1 / cols) round identically when cols is a power of two
   const bool pow2 = (a.cols & (a.cols - 1)) == 0;
   double cx = 0.0, cy = 0.0;  // HILBERT_SCHMIDT_TEST / INFIDELITY: grad = cx t.x - cy t.y
   if (a.variant == SQG_FROBENIUS_NORM) {
-    f = 1.0 - tr.x / dc;
+    f = 1.0 - (pow2 ? tr.x * inv_dc : tr.x / dc);
   } else if (a.variant == SQG_HILBERT_SCHMIDT_TEST) {
     double d = 1.0 / dc;
     f = 1.0 - d * d * (tr.x * tr.x + tr.y * tr.y);
@@ -631,11 +632,11 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
     norm_Z = fmin(norm_Z, t);
     norm_Z = fmax(norm_Z, t * 0.1);
   }
-  const double sdt = sqrt(dtg);
+  const double isdt = 1.0 / sqrt(dtg), idtg = 1.0 / dtg;
   __syncthreads();
   double c0 = 0.0;
   for (int r = threadIdx.x; r < P; r += blockDim.x) {
-    const double z0 = fabs(sh.delta[r]) > kNumPrecision ? sh.delta[r] / sdt : 0.0;
+    const double z0 = fabs(sh.delta[r]) > kNumPrecision ? sh.delta[r] * isdt : 0.0;
     Z[(long long)r * P] = z0;
     c0 = fma(z0, sh.g[r], c0);
   }
@@ -649,7 +650,7 @@ __device__ double dec_bfgs_update(const DecArgs& a, const Sh& sh, double norm_Z)
       sh.zs[0] = c0;
       continue;
     }
-    const double cs = sh.cs[c], gtz = sh.vp[c] / dtg, gc = gtz / cs;
+    const double cs = sh.cs[c], gtz = sh.vp[c] * idtg, gc = gtz / cs;
     double s = 0.0;
     for (int r0 = 0; r0 < P; r0 += kChunk) {
       double zv[kChunk];
@@ -714,11 +715,13 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
     double dg = dot(sh.d, sh.g, P, sh.scratch);
     double max_step = 0.0;
     if (dg < 0.0) {
-      double ms = INFINITY;
+      // min_k |2 pi / d_k| over |d_k| >= 1e-5 (grad_descend.cpp:399-425) is 2 pi / max_k |d_k|:
+      // correctly rounded division is monotone, so one division gives the same value
+      double dmax = 0.0;
       for (int k = threadIdx.x; k < P; k += blockDim.x)
-        if (fabs(sh.d[k]) >= 1e-5) ms = fmin(ms, fabs(kTwoPi / sh.d[k]));
-      ms = block_allmin(ms, sh.scratch);
-      max_step = isinf(ms) ? 0.0 : ms;
+        if (fabs(sh.d[k]) >= 1e-5) dmax = fmax(dmax, fabs(sh.d[k]));
+      dmax = -block_allmin(-dmax, sh.scratch);
+      max_step = dmax > 0.0 ? kTwoPi / dmax : 0.0;
     }
     double gn = dot(sh.g, sh.g, P, sh.scratch);
     if (gn <= 1e-19 * 1e-19 || dg >= 0.0 || f >= fprev) break;
@@ -1132,6 +1135,7 @@ int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, v
 
 // Evaluation form of the decomposition kernels for this circuit and target width.
 void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
+  a.inv_cols = 1.0 / cols;
   a.cyclic = use_cyclic(c, cols) ? 1 : 0;
   a.chains = 1;
   a.split = 0;
