@@ -932,17 +932,13 @@ __device__ double dec_adam(const DecArgs& a, const Sh& sh, int b, int& calls, in
   return cur_min;
 }
 
-// At most 80 registers (6 CTAs of 128 threads per SM): the evaluation keeps only one warp
-// per CTA busy at n = 3, so resident CTAs are what hides FP64 and shared-memory latency
-// (measured 7470 vs 7103 decompositions/s with the unconstrained 126 registers).
-template <int OPT, int FORM>
-__global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
-  extern __shared__ double2 smem2[];
-  const int b = blockIdx.x;
-  if (b >= a.B) return;
+// Shared-memory layout common to the decomposition and evaluation kernels (dec_smem_bytes
+// without the optimizer's own part): gate list, target of instance b, state matrices, gate
+// matrices, per-gate overlaps, parameter maps, kDecVectors P-vectors and reduction scratch.
+// Loads the gate list and the target; returns the first free byte.  The caller
+// synchronises before use.
+__device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
   const int P = a.P, L = a.L, NC = a.N * a.cols;
-  Sh sh;
-  char* p = reinterpret_cast<char*>(smem2);
   auto take = [&](size_t bytes) { char* r = p; p += (bytes + 15) / 16 * 16; return r; };
   Gate* gsh = (Gate*)take(sizeof(Gate) * max(L, 1));
   sh.gates = gsh;
@@ -968,6 +964,45 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   sh.redd = (double*)take(sizeof(double) * kTileMaxWarps * 8);
   sh.tot = (double*)take(sizeof(double) * 8);
   sh.scratch = (double*)take(sizeof(double) * kTileMaxWarps);
+  sh.Z = nullptr;
+  for (int e = threadIdx.x; e < NC; e += blockDim.x) tsh[e] = a.targets[(long long)b * a.tstride + e];
+  for (int g = threadIdx.x; g < L; g += blockDim.x) {
+    const Gate gt = a.gates[g];
+    gsh[g] = gt;
+    for (int k = 0; k < gate_param_num(gt.type); k++) sh.pgate[gt.pstart + k] = g;
+  }
+  return p;
+}
+
+// Batched cost and gradient through the environment-matrix evaluation, one CTA per
+// parameter vector b (theta row b, target b * a.tstride; tstride 0 shares one target).
+template <int FORM>
+__global__ void __launch_bounds__(kDecThreads, 6) k_env_costgrad(DecArgs a, const double* __restrict__ theta,
+                                                                 double* __restrict__ cost, double* __restrict__ grad) {
+  extern __shared__ double2 smem2[];
+  const int b = blockIdx.x;
+  if (b >= a.B) return;
+  Sh sh;
+  dec_setup(a, sh, b, reinterpret_cast<char*>(smem2));
+  for (int i = threadIdx.x; i < a.P; i += blockDim.x) sh.x[i] = theta[(long long)b * a.P + i];
+  __syncthreads();
+  const double f = dec_eval<FORM>(a, sh, sh.x, sh.g, b);
+  for (int i = threadIdx.x; i < a.P; i += blockDim.x) grad[(long long)b * a.P + i] = sh.g[i];
+  if (threadIdx.x == 0) cost[b] = f;
+}
+
+// At most 80 registers (6 CTAs of 128 threads per SM): the evaluation keeps only one warp
+// per CTA busy at n = 3, so resident CTAs are what hides FP64 and shared-memory latency
+// (measured 7470 vs 7103 decompositions/s with the unconstrained 126 registers).
+template <int OPT, int FORM>
+__global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
+  extern __shared__ double2 smem2[];
+  const int b = blockIdx.x;
+  if (b >= a.B) return;
+  const int P = a.P;
+  Sh sh;
+  char* p = dec_setup(a, sh, b, reinterpret_cast<char*>(smem2));
+  auto take = [&](size_t bytes) { char* r = p; p += (bytes + 15) / 16 * 16; return r; };
   double* f0_vec = nullptr;
   int* dec_vec = nullptr;
   if (OPT == kAdam) {
@@ -978,12 +1013,6 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     sh.Z = a.z_in_smem ? (double*)take(sizeof(double) * P * P) : a.zglob + (long long)b * P * P;
   }
 
-  for (int e = threadIdx.x; e < NC; e += blockDim.x) tsh[e] = a.targets[(long long)b * a.tstride + e];
-  for (int g = threadIdx.x; g < L; g += blockDim.x) {
-    Gate gt = a.gates[g];
-    gsh[g] = gt;
-    for (int k = 0; k < gate_param_num(gt.type); k++) sh.pgate[gt.pstart + k] = g;
-  }
   for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = a.x[(long long)b * P + i];
   __syncthreads();
   double best = INFINITY;
@@ -1146,6 +1175,49 @@ void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
 }
 
 }  // namespace
+
+namespace sqg {
+
+template <int FORM>
+static int env_launch(const DecArgs& a, const double* theta, double* cost, double* grad, int threads, size_t smem,
+                      cudaStream_t s) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_env_costgrad<FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  k_env_costgrad<FORM><<<a.B, threads, smem, s>>>(a, theta, cost, grad);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_env_costgrad: ") + cudaGetErrorString(e));
+}
+
+// Cost and gradient of B parameter vectors (B x P, contiguous) of a circuit of at most five
+// qubits against targets with cols >= 3N/4 columns, one CTA per vector with the
+// environment-matrix evaluation of the decomposition kernel.  Returns SQG_ERR_UNSUPPORTED
+// (without launching) for shapes it does not take; sqg_cost_grad then uses the tile kernels.
+int env_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* target, int cols, long long tstride,
+                  int off, int variant, double* cost, double* grad, void* stream) {
+  const char* f = getenv("SQG_COSTGRAD_FORM");
+  if (f && std::string(f) == "tile") return SQG_ERR_UNSUPPORTED;
+  if (c->n > 5 || c->P == 0 || c->L == 0 || !grad || !use_cyclic(c, cols)) return SQG_ERR_UNSUPPORTED;
+  const size_t smem = dec_smem_bytes(c, cols, false, false);
+  if (smem > 100 * 1024) return SQG_ERR_UNSUPPORTED;
+  DecArgs a = {};
+  a.gates = c->d_gates;
+  a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N; a.cols = cols;
+  a.trace_offset = off;
+  a.variant = variant;
+  a.targets = (const double2*)target;
+  a.tstride = tstride;
+  a.B = B;
+  dec_eval_form(c, cols, off, a);
+  const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
+  cudaStream_t s = (cudaStream_t)stream;
+  if (a.chains == 2) return env_launch<kFormTwoChains>(a, theta, cost, grad, threads, smem, s);
+  return env_launch<kFormCyclic>(a, theta, cost, grad, threads, smem, s);
+}
+
+}  // namespace sqg
 
 extern "C" {
 

@@ -564,6 +564,12 @@ int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* 
   const bool with_grad = grad != nullptr && c->P > 0;
   if (with_grad && c->n > 12) return fail(SQG_ERR_UNSUPPORTED, "gradient supports qbit_num <= 12");
   if (checkpoint_interval < 0) return fail(SQG_ERR_INVALID_ARGUMENT, "negative checkpoint interval");
+  if (with_grad && checkpoint_interval == 0) {
+    // up to five qubits: one CTA per vector with the environment-matrix evaluation
+    st = sqg::env_cost_grad(c, theta, B, target, cols, target_batch_stride, off, variant, cost, grad, stream);
+    if (st != SQG_ERR_UNSUPPORTED) return st;
+    st = SQG_OK;
+  }
   EvalLayout l = eval_layout(c, B, cols, with_grad, with_grad ? checkpoint_interval : 0);
   if (!workspace || ws_bytes < l.end) return fail(SQG_ERR_WORKSPACE, "workspace too small: need " + std::to_string(l.end));
   cudaStream_t s = (cudaStream_t)stream;

@@ -30,4 +30,8 @@ struct sqg_circuit {
 namespace sqg {
 // Records msg as the calling thread's last error and returns status.
 int set_error(int status, const std::string& msg);
+// Environment-matrix cost and gradient for qbit_num <= 5 (decompose.cu); SQG_ERR_UNSUPPORTED
+// for shapes it does not take.
+int env_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* target, int cols, long long tstride,
+                  int off, int variant, double* cost, double* grad, void* stream);
 }  // namespace sqg
