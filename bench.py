@@ -114,6 +114,14 @@ def flush_l2(buf):
     buf.add_(1)
 
 
+def barrier():
+    """Barrier across the ranks of a torchrun launch (no-op for a single process)."""
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
 def fp64_ops_per_eval(circuit_records, N, cols):
     """FP64 instructions of one cost+gradient evaluation in the tile kernels (update
     rules of gates.cuh): forward per pair U3 14, RX/RY/RZ 8, CRY 8 on the controlled
@@ -226,6 +234,7 @@ def bench_ours(args):
     clocks.start()
     times, solved, calls_tot, iters_tot = [], 0, 0, 0
     torch.cuda.synchronize()
+    barrier()
     for k in range(args.steps):
         flush_l2(flush)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -240,6 +249,7 @@ def bench_ours(args):
         calls_tot += int(calls.cpu().numpy().astype(np.int64).sum())
         iters_tot += int(dec.iters.cpu().numpy().astype(np.int64).sum())
     torch.cuda.synchronize()
+    barrier()
     clk = clocks.stop()
     t_total = sum(times)
     value = solved / t_total
