@@ -54,8 +54,7 @@ int cuda_status(cudaError_t e, const char* where) {
 }
 
 constexpr int kMaxThreads = 256;
-constexpr int kMaxWarps = kMaxThreads / 32;
-constexpr size_t kSmemBudgetFwd = 100 * 1024;   // column tile budget, forward only (n = 12: one column, 2 CTAs/SM)
+constexpr size_t kSmemBudgetFwd = 100 * 1024;   // column tile budget, forward only (n = 12: one column, 3 CTAs/SM)
 constexpr size_t kSmemBudgetGrad = 100 * 1024;  // psi + lambda tiles
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }

@@ -330,3 +330,30 @@ def test_dropin_adam_above_five_qubits_follows_the_oracle(sqg):
     dec.set_Optimized_Parameters(x0)
     dec.Start_Decomposition()
     assert dec.get_Decomposition_Error() <= fg_orc + 1e-9
+
+
+@pytest.mark.parametrize("n,cols,offset,variant", [(2, 4, 0, 0), (3, 8, 0, 0), (3, 6, 2, 0), (4, 16, 0, 3),
+                                                   (4, 12, 4, 0), (4, 16, 0, 9)])
+def test_small_register_cost_grad_forms_agree(sqg, monkeypatch, n, cols, offset, variant):
+    """Up to five qubits sqg_cost_grad evaluates gradients with the environment-matrix kernel;
+    it matches the oracle and the tile kernels (SQG_COSTGRAD_FORM=tile)."""
+    import importlib
+
+    wl = importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+    rng = np.random.default_rng(300 + n + cols)
+    c = wl.all_gates_circuit(n, 30, rng)
+    P = c.get_Parameter_Num()
+    U = O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, P))
+    T = np.ascontiguousarray(U.conj().T[:, offset:offset + cols])
+    th = rng.uniform(0, 2 * np.pi, (5, P))
+    off = offset if variant == 0 else 0
+    ev = sqg.CostEvaluator(c, T, trace_offset=off, cost_variant=variant)
+    ce, ge = ev.cost_grad(torch.from_numpy(th).cuda())
+    monkeypatch.setenv("SQG_COSTGRAD_FORM", "tile")
+    ct, gt = ev.cost_grad(torch.from_numpy(th).cuda())
+    torch.cuda.synchronize()
+    cr, gr = O.batch(n, c.gate_records(), th, T, trace_offset=off, variant=variant, with_grad=True)
+    scale = max(1.0, float(np.abs(gr).max()))
+    for cost, grad in ((ce, ge), (ct, gt)):
+        assert np.allclose(cost.cpu().numpy(), cr, rtol=0, atol=1e-12)
+        assert float(np.abs(grad.cpu().numpy() - gr).max()) <= 1e-12 * scale
