@@ -3,12 +3,14 @@
 // initialiser's layer GEMMs.  C[M][N] = A[M][K] * B[N][K]^T (+ bias[n], optional ReLU),
 // both operands K-major bf16, FP32 accumulation; results as fp32 and/or bf16.
 //
-// One CTA computes a 128 x 128 tile: warp 0 allocates 128 TMEM columns, thread 0 issues
-// the TMA loads (two pipeline stages of 128 x 64 for A and B) and the MMAs
-// (4 x K=16 per stage), each stage's MMAs are committed to an mbarrier that frees the
-// stage; finally the four warps read their 32 TMEM lanes each (32x32b loads) and apply the
-// epilogue.  Every mbarrier wait is bounded: on a time-out the CTA records an error code,
-// drains its own copies and MMAs (again bounded), frees its TMEM and returns.
+// One CTA computes a 128 x 128 tile: warp 0 allocates 128 TMEM columns; one thread of warp
+// 0 issues the TMA loads into a ring of four stages (128 x 64 of A and of B each) and waits
+// only for a stage's "empty" barrier, one thread of warp 1 issues the MMAs (4 x K=16 per
+// stage) and commits each stage to that barrier; finally the four warps read their 32 TMEM
+// lanes each (32x32b loads) into a padded shared-memory tile and store it row by row
+// (coalesced), with the bias / ReLU epilogue.  Every mbarrier wait is bounded: on a
+// time-out the CTA records an error code, drains its own copies and MMAs (again bounded),
+// frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -21,8 +23,10 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 64, STAGES = 2;
+constexpr int TM = 128, TN = 128, TK = 64, STAGES = 4;
 constexpr int STAGE_BYTES = (TM + TN) * TK * 2;  // 32 KB
+constexpr int EPI_LD = TN + 1;                   // fp32 epilogue tile row (odd: no bank conflicts)
+static_assert(TM * EPI_LD * 4 <= STAGES * STAGE_BYTES, "the epilogue tile reuses the stage buffers");
 constexpr unsigned kSpinLimit = 1u << 24;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -80,20 +84,22 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
   extern __shared__ __align__(1024) unsigned char dsmem[];
   // 1024-byte alignment for the swizzled tiles
   unsigned char* base = (unsigned char*)(((unsigned long long)dsmem + 1023) & ~1023ull);
-  __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_done[STAGES], bar_final;
+  __shared__ __align__(8) unsigned long long bar_full[STAGES], bar_empty[STAGES], bar_final;
   __shared__ unsigned tmem_base_s;
-  __shared__ int failed_s;
-  const int warp = threadIdx.x >> 5;
+  __shared__ int failed_s, issued_s, consumed_s, final_ok_s;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
   const int ktiles = (K + TK - 1) / TK;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(smem_u32(&bar_full[s]), 1);
-      mbar_init(smem_u32(&bar_done[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
     }
     mbar_init(smem_u32(&bar_final), 1);
     failed_s = 0;
+    issued_s = 0;
+    consumed_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -105,23 +111,32 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const unsigned tmem = tmem_base_s;
   const unsigned idesc = instr_desc(TM, TN);
+  volatile int* failed = &failed_s;
 
-  if (threadIdx.x == 0) {
-    bool ok = true;
-    int issued = 0;  // TMA stages issued
-    int committed = 0;
-    // prologue: fill the pipeline
-    for (; issued < ktiles && issued < STAGES; issued++) {
-      unsigned sa = smem_u32(base + issued * STAGE_BYTES), sb = sa + TM * TK * 2;
-      unsigned bf = smem_u32(&bar_full[issued]);
+  if (warp == 0 && lane == 0) {
+    // TMA producer: fills stage s again once the MMAs that read it have completed
+    int issued = 0;
+    for (int kt = 0; kt < ktiles && !*failed; kt++) {
+      const int s = kt % STAGES;
+      if (kt >= STAGES && !mbar_wait(smem_u32(&bar_empty[s]), ((kt / STAGES) - 1) & 1)) {
+        *failed = 1;
+        break;
+      }
+      const unsigned sa = smem_u32(base + s * STAGE_BYTES), sb = sa + TM * TK * 2;
+      const unsigned bf = smem_u32(&bar_full[s]);
       mbar_expect_tx(bf, STAGE_BYTES);
-      tma_load_2d(sa, &mapA, issued * TK, m0, bf);
-      tma_load_2d(sb, &mapB, issued * TK, n0, bf);
+      tma_load_2d(sa, &mapA, kt * TK, m0, bf);
+      tma_load_2d(sb, &mapB, kt * TK, n0, bf);
+      issued++;
     }
-    for (int kt = 0; kt < ktiles && ok; kt++) {
+    issued_s = issued;
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer: four K = 16 MMAs per stage, each stage committed to its empty barrier
+    int consumed = 0;
+    for (int kt = 0; kt < ktiles && !*failed; kt++) {
       const int s = kt % STAGES;
       if (!mbar_wait(smem_u32(&bar_full[s]), (kt / STAGES) & 1)) {
-        ok = false;
+        *failed = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -136,43 +151,32 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
             "l"(da), "l"(db), "r"(idesc), "r"(acc));
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(&bar_done[s]))
+                       smem_u32(&bar_empty[s]))
                    : "memory");
-      committed = kt + 1;
-      // refill this stage once its MMAs are done
-      if (issued < ktiles) {
-        if (!mbar_wait(smem_u32(&bar_done[s]), (kt / STAGES) & 1)) {
-          ok = false;
-          break;
-        }
-        unsigned bf = smem_u32(&bar_full[s]);
-        mbar_expect_tx(bf, STAGE_BYTES);
-        tma_load_2d(sa, &mapA, issued * TK, m0, bf);
-        tma_load_2d(sb, &mapB, issued * TK, n0, bf);
-        issued++;
-      }
+      consumed++;
     }
-    if (ok) {
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(&bar_final))
-                   : "memory");
-    } else {
-      failed_s = 1;
-      atomicExch(err, 1);
-      // drain: wait (bounded) for the copies and MMAs this CTA issued
-      for (int kt = committed; kt < issued; kt++) mbar_wait(smem_u32(&bar_full[kt % STAGES]), (kt / STAGES) & 1);
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(&bar_final))
-                   : "memory");
-    }
+    consumed_s = consumed;
+    // completion of every MMA issued above (also after a time-out)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(&bar_final))
+                 : "memory");
   }
-  __shared__ int final_ok_s;
-  if (threadIdx.x == 0) final_ok_s = mbar_wait(smem_u32(&bar_final), 0) ? 1 : 0;
   __syncthreads();
-  const bool done = final_ok_s != 0;  // CTA-uniform: the TMEM loads below are warp-collective
+  if (threadIdx.x == 0) {
+    if (failed_s) {
+      atomicExch(err, 1);
+      // drain: wait (bounded) for the copies issued but not consumed by an MMA
+      for (int kt = consumed_s; kt < issued_s; kt++) mbar_wait(smem_u32(&bar_full[kt % STAGES]), (kt / STAGES) & 1);
+    }
+    final_ok_s = mbar_wait(smem_u32(&bar_final), 0) ? 1 : 0;
+    if (!final_ok_s) atomicExch(err, 2);
+  }
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (done && !failed_s) {
-    const int row = m0 + warp * 32 + (threadIdx.x & 31);
+  if (final_ok_s && !failed_s) {
+    // every MMA has completed: the stage buffers hold the fp32 tile for coalesced stores
+    float* epi = reinterpret_cast<float*>(base);
+    const int r = warp * 32 + lane;
 #pragma unroll 1
     for (int c0 = 0; c0 < TN; c0 += 32) {
       unsigned v[32];
@@ -186,22 +190,23 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
             "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < M) {
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-          const int col = n0 + c0 + j;
-          if (col < N) {
-            float x = __uint_as_float(v[j]);
-            if (bias) x += bias[col];
-            if (relu) x = fmaxf(x, 0.f);
-            if (C) C[(long long)row * ldc + col] = x;
-            if (Cb) Cb[(long long)row * ldc + col] = __float2bfloat16(x);
-          }
-        }
+      for (int j = 0; j < 32; j++) epi[r * EPI_LD + c0 + j] = __uint_as_float(v[j]);
+    }
+    __syncthreads();
+    for (int rr = warp; rr < TM; rr += 4) {
+      const int row = m0 + rr;
+      if (row >= M) continue;
+      for (int c = lane; c < TN; c += 32) {
+        const int col = n0 + c;
+        if (col >= N) continue;
+        float x = epi[rr * EPI_LD + c];
+        if (bias) x += bias[col];
+        if (relu) x = fmaxf(x, 0.f);
+        if (C) C[(long long)row * ldc + col] = x;
+        if (Cb) Cb[(long long)row * ldc + col] = __float2bfloat16(x);
       }
     }
-  } else if (!done && threadIdx.x == 0) {
-    atomicExch(err, 2);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
