@@ -118,6 +118,16 @@ class Circuit:
             p += PARAM_NUM[t]
         return out
 
+    def Remap_Qbits(self, qbit_map):
+        """New circuit with every qubit q moved to qbit_map[q] (a permutation)."""
+        m = [int(v) for v in qbit_map]
+        if sorted(m) != list(range(self.qbit_num)):
+            raise ValueError("qbit_map must be a permutation of the qubits")
+        out = Circuit(self.qbit_num)
+        for t, tg, c in self._gates:
+            out._add(t, m[tg], m[c] if c >= 0 else -1)
+        return out
+
     def get_Gate_Nums(self):
         nums = {}
         for t, _, _ in self._gates:

@@ -158,6 +158,96 @@ class N_Qubit_Decomposition_custom:
     def set_Convergence_Threshold(self, threshold):
         self.config["convergence_threshold"] = float(threshold)
 
+    # ---- bookkeeping methods of the reference wrapper (DECOMPOSITION_WRAPPER_BASE_METHODS,
+    # qgd_N_Qubit_Decompositions_Wrapper.cpp) ------------------------------------------------
+    def get_Gates(self):
+        """Gate dictionaries with the optimized parameters (Wrapper get_Gates: "type",
+        "target_qbit", "control_qbit", U3 "Theta"/"Phi"/"Lambda", RX/RY/CRY "Theta", RZ "Phi")."""
+        out = []
+        params = self.optimized_parameters
+        for d in self.circuit.get_Gates():
+            g = {"type": d["type"], "target_qbit": d["target_qbit"]}
+            if "control_qbit" in d:
+                g["control_qbit"] = d["control_qbit"]
+            ps = d["parameter_start_index"]
+            if d["type"] == "U3" and params.size >= ps + 3:
+                g["Theta"], g["Phi"], g["Lambda"] = float(params[ps]), float(params[ps + 1]), float(params[ps + 2])
+            elif d["type"] in ("RX", "RY", "CRY") and params.size >= ps + 1:
+                g["Theta"] = float(params[ps])
+            elif d["type"] == "RZ" and params.size >= ps + 1:
+                g["Phi"] = float(params[ps])
+            out.append(g)
+        return out
+
+    def List_Gates(self):
+        """Prints the gate structure with the optimized parameters."""
+        for k, g in enumerate(self.get_Gates()):
+            print("%d-th gate: %s" % (k, ", ".join("%s %s" % (key, val) for key, val in g.items())))
+
+    def get_Project_Name(self):
+        return getattr(self, "project_name", "")
+
+    def set_Project_Name(self, name):
+        self.project_name = str(name)
+
+    def set_Debugfile(self, filename):
+        self.debugfile = str(filename)
+
+    def set_Max_Layer_Num(self, max_layer_num):
+        """Stored for structure-building decompositions; a custom gate structure is used as given."""
+        self.max_layer_num = max_layer_num
+
+    def set_Optimization_Blocks(self, optimization_blocks):
+        """Stored; the custom decomposition optimizes all gates of the structure at once."""
+        self.optimization_blocks = int(optimization_blocks)
+
+    def get_Global_Phase(self):
+        gp = getattr(self, "global_phase_factor", 1.0 + 0.0j)
+        return math.atan2(gp.imag, gp.real)
+
+    def set_Global_Phase(self, phase):
+        """Decomposition_Base::set_global_phase (Decomposition_Base.cpp:1098-1101), including
+        its sqrt(2) magnitude."""
+        self.global_phase_factor = complex(math.sqrt(2) * math.cos(phase), math.sqrt(2) * math.sin(phase))
+
+    def apply_Global_Phase_Factor(self):
+        """Multiplies the target by the global phase factor and resets the phase
+        (Decomposition_Base.cpp:1117-1121)."""
+        self.Umtx = np.ascontiguousarray(self.Umtx * getattr(self, "global_phase_factor", 1.0 + 0.0j))
+        self.set_Global_Phase(0)
+        self._evaluator = None
+
+    def export_Unitary(self, filename):
+        """Decomposition_Base::export_unitary (Decomposition_Base.cpp:1128-1143): int32 rows,
+        int32 cols, then the complex128 entries row by row, the project name prefixed."""
+        name = str(filename)
+        if self.get_Project_Name():
+            name = self.get_Project_Name() + "_" + name
+        with open(name, "wb") as f:
+            np.asarray([self.Umtx.shape[0], self.Umtx.shape[1]], dtype=np.int32).tofile(f)
+            np.ascontiguousarray(self.Umtx, dtype=np.complex128).tofile(f)
+
+    def Reorder_Qubits(self, qbit_list):
+        """Decomposition_Base::reorder_qubits (Decomposition_Base.cpp:910-950) with
+        Gate::reorder_qubits (Gate.cpp:1151-1195): qubit qbit_list[k] becomes qubit k, in the
+        gate structure and in the rows and columns of the target."""
+        ql = [int(q) for q in qbit_list]
+        n = self.qbit_num
+        if sorted(ql) != list(range(n)):
+            raise ValueError("Gate::reorder_qubits: Wrong number of qubits.")
+        new_of_old = [0] * n
+        for k, q in enumerate(ql):
+            new_of_old[q] = k
+        self.circuit = self.circuit.Remap_Qbits(new_of_old)
+        idx = np.arange(self.Umtx.shape[0])
+        perm = np.zeros_like(idx)
+        for k, q in enumerate(ql):
+            perm |= ((idx >> q) & 1) << k
+        U = np.empty_like(self.Umtx)
+        U[np.ix_(perm, perm)] = self.Umtx
+        self.Umtx = U
+        self._evaluator = None
+
     # ---- cost / gradient -----------------------------------------------------------------
     def evaluator(self):
         if self._evaluator is None:

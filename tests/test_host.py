@@ -173,3 +173,38 @@ def test_vectorised_target_generators(sqg):
     c.add_U3(ctl)
     c.add_U3(tgt)
     assert np.allclose(one, wl.circuit_matrix(c, np.concatenate([p0, p1, pc, pt])), atol=1e-12)
+
+
+def test_dropin_bookkeeping_methods(sqg, tmp_path):
+    """get_Gates / Reorder_Qubits / global phase / export_Unitary of the decomposition class
+    follow the reference wrapper's base methods (qgd_N_Qubit_Decompositions_Wrapper.cpp)."""
+    wl = importlib.import_module("sequential-quantum-gate-decomposer_gb300.workloads")
+    c = wl.cnot_u3_ansatz(3, 2)
+    P = c.get_Parameter_Num()
+    p = np.random.default_rng(2).uniform(0, 2 * np.pi, P)
+    U = O.get_matrix(3, c.gate_records(), p)
+    d = sqg.N_Qubit_Decomposition_custom(np.ascontiguousarray(U.conj().T))
+    d.set_Gate_Structure(c)
+    d.set_Optimized_Parameters(p)
+    g = d.get_Gates()
+    assert g[0]["type"] == "U3" and g[0]["Theta"] == p[0] and g[0]["Lambda"] == p[2]
+    assert any(x["type"] == "CNOT" and "control_qbit" in x and "Theta" not in x for x in g)
+    # reordering the qubits of both the structure and the target keeps the cost at zero
+    d.Reorder_Qubits([2, 0, 1])
+    assert abs(O.cost(3, d.get_Circuit().gate_records(), p, d.get_Unitary())) < 1e-12
+    with pytest.raises(ValueError):
+        d.Reorder_Qubits([0, 0, 1])
+    # global phase: set_global_phase stores sqrt(2) e^{i phi}; apply multiplies the target
+    d.set_Global_Phase(0.25)
+    assert d.get_Global_Phase() == pytest.approx(0.25)
+    before = d.get_Unitary()
+    d.apply_Global_Phase_Factor()
+    assert np.allclose(d.get_Unitary(), before * np.sqrt(2) * np.exp(0.25j))
+    assert d.get_Global_Phase() == 0.0
+    # export_Unitary: int32 rows, int32 cols, complex128 entries, project-name prefix
+    d.set_Project_Name(str(tmp_path / "proj"))
+    d.export_Unitary("u.bin")
+    raw = np.fromfile(str(tmp_path / "proj") + "_u.bin", dtype=np.uint8)
+    dims = raw[:8].view(np.int32)
+    assert list(dims) == [8, 8]
+    assert np.array_equal(raw[8:].view(np.complex128).reshape(8, 8), d.get_Unitary())
