@@ -118,15 +118,46 @@ class Circuit:
             p += PARAM_NUM[t]
         return out
 
-    def Remap_Qbits(self, qbit_map):
-        """New circuit with every qubit q moved to qbit_map[q] (a permutation)."""
-        m = [int(v) for v in qbit_map]
-        if sorted(m) != list(range(self.qbit_num)):
-            raise ValueError("qbit_map must be a permutation of the qubits")
-        out = Circuit(self.qbit_num)
+    def Remap_Qbits(self, qbit_map, qbit_num=None):
+        """New circuit with qubit q of every gate moved to qbit_map[q] (a dict {initial:
+        remapped} as in qgd_Circuit.Remap_Qbits, or a sequence), on qbit_num qubits
+        (default: this circuit's)."""
+        n = self.qbit_num if qbit_num is None else int(qbit_num)
+        m = dict(qbit_map) if isinstance(qbit_map, dict) else {q: int(v) for q, v in enumerate(qbit_map)}
+        out = Circuit(n)
         for t, tg, c in self._gates:
-            out._add(t, m[tg], m[c] if c >= 0 else -1)
+            if tg not in m or (c >= 0 and c not in m):
+                raise ValueError("qbit_map does not cover every qubit of the circuit")
+            out._add(t, int(m[tg]), int(m[c]) if c >= 0 else -1)
         return out
+
+    def get_Qbits(self):
+        """Sorted qubit indices the gates act on."""
+        return sorted({q for _, tg, c in self._gates for q in ((tg, c) if c >= 0 else (tg,))})
+
+    def _gate_qubits(self, k):
+        _, tg, c = self._gates[k]
+        return (tg, c) if c >= 0 else (tg,)
+
+    def get_Parents(self, gate):
+        """Indices of the gates that last act, before gate `gate`, on each of its qubits."""
+        out = set()
+        for q in self._gate_qubits(gate):
+            for k in range(gate - 1, -1, -1):
+                if q in self._gate_qubits(k):
+                    out.add(k)
+                    break
+        return sorted(out)
+
+    def get_Children(self, gate):
+        """Indices of the gates that next act, after gate `gate`, on each of its qubits."""
+        out = set()
+        for q in self._gate_qubits(gate):
+            for k in range(gate + 1, len(self._gates)):
+                if q in self._gate_qubits(k):
+                    out.add(k)
+                    break
+        return sorted(out)
 
     def get_Gate_Nums(self):
         nums = {}

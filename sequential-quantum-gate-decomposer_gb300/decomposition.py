@@ -238,7 +238,7 @@ class N_Qubit_Decomposition_custom:
         new_of_old = [0] * n
         for k, q in enumerate(ql):
             new_of_old[q] = k
-        self.circuit = self.circuit.Remap_Qbits(new_of_old)
+        self.circuit = self.circuit.Remap_Qbits({q: new_of_old[q] for q in range(n)})
         idx = np.arange(self.Umtx.shape[0])
         perm = np.zeros_like(idx)
         for k, q in enumerate(ql):

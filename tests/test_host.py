@@ -208,3 +208,22 @@ def test_dropin_bookkeeping_methods(sqg, tmp_path):
     dims = raw[:8].view(np.int32)
     assert list(dims) == [8, 8]
     assert np.array_equal(raw[8:].view(np.complex128).reshape(8, 8), d.get_Unitary())
+
+
+def test_circuit_structure_queries(sqg):
+    """Remap_Qbits (dict form, other qubit count), get_Qbits, get_Parents / get_Children."""
+    c = sqg.Circuit(3)
+    c.add_U3(0)        # 0
+    c.add_CNOT(1, 0)   # 1: target 1, control 0
+    c.add_RY(2)        # 2
+    c.add_CRY(2, 1)    # 3
+    c.add_U3(0)        # 4
+    assert c.get_Qbits() == [0, 1, 2]
+    assert c.get_Parents(1) == [0] and c.get_Parents(3) == [1, 2] and c.get_Parents(4) == [1]
+    assert c.get_Children(0) == [1] and c.get_Children(1) == [3, 4] and c.get_Children(4) == []
+    r = c.Remap_Qbits({0: 3, 1: 1, 2: 0}, 4)
+    assert r.qbit_num == 4
+    assert [(g["target_qbit"], g.get("control_qbit", -1)) for g in r.get_Gates()] == [(3, -1), (1, 3), (0, -1), (0, 1),
+                                                                                         (3, -1)]
+    with pytest.raises(ValueError):
+        c.Remap_Qbits({0: 1})
