@@ -228,6 +228,29 @@ int sqg_decompose_batched_adam(const sqg_circuit* circuit, const void* targets_d
                                int random_shift_count_max, long long randomization_threshold, int max_outer,
                                unsigned long long seed, void* stream);
 
+/* One decomposition with SQUANDER's ADAM engine for any qbit_num the gradient supports
+ * (<= 12), run on the device as a single CUDA graph launch: a conditional while-node whose
+ * body evaluates the cost and gradient (the kernels of sqg_cost_grad) and then takes one
+ * pass of the engine loop on one CTA, with no host round trip between evaluations.  Replaces
+ * the host loop of Optimization_Interface::solve_layer_optimization_problem_ADAM
+ * (src-cpp/optimization_engines/ADAM.cpp:44-330), the optimizer
+ * N_Qubit_Decomposition_custom selects above five qubits (N_Qubit_Decomposition_custom.cpp:
+ * 59-76).  The engine's semantics and parameters are those of sqg_decompose_batched_adam
+ * with batch 1; current_minimum is the running minimum the first engine call starts with
+ * (Decomposition_Base's current_minimum; DBL_MAX for a fresh decomposition), and the random
+ * numbers come from a splitmix64 stream seeded with seed.  target_dev is N x cols (U dagger),
+ * x_dev (P) holds the start point on entry and the best point on exit; cost_dev, evals_dev
+ * and shifts_dev (nullable) are single values.  The workspace (256-byte aligned,
+ * sqg_adam_loop_workspace_bytes) holds the engine state and the evaluation scratch and must
+ * stay untouched until the stream reaches the end of the call.  Asynchronous on stream. */
+size_t sqg_adam_loop_workspace_bytes(const sqg_circuit* circuit, int cols);
+int sqg_decompose_adam_loop(const sqg_circuit* circuit, const void* target_dev, int cols, int trace_offset,
+                            int cost_variant, double* x_dev, double* cost_dev, int* evals_dev, int* shifts_dev,
+                            double tolerance, int max_iters, double eta, int adaptive_eta,
+                            int random_shift_count_max, long long randomization_threshold, int max_outer,
+                            double current_minimum, unsigned long long seed, void* workspace_dev,
+                            size_t workspace_bytes, void* stream);
+
 /* Measures the FP64 FMA peak of the current device in TFLOP/s (an FMA counts 2 flops) with
  * independent DFMA chains on 8 CTAs per SM, timed with CUDA events; scratch_dev receives
  * the chains' results (sqg_probe_fp64_scratch_bytes() bytes).  With active_lanes < 32 only

@@ -17,7 +17,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 LIB_PATH = os.path.join(PKG_DIR, "libsqg.so")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
-CU_SOURCES = ["engine.cu", "decompose.cu", "probe.cu", "mlp.cu", "ragged.cu", "gemm_tc.cu"]
+CU_SOURCES = ["engine.cu", "decompose.cu", "loop.cu", "probe.cu", "mlp.cu", "ragged.cu", "gemm_tc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -126,6 +126,11 @@ def _declare(lib):
     lib.sqg_apply_state.argtypes = [vp, vp, c_int, vp, c_ll, c_int, vp, c_sz, vp]
     lib.sqg_decompose_batched_adam.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double,
                                                c_int, ctypes.c_double, c_int, c_int, c_ll, c_int, ctypes.c_uint64, vp]
+    lib.sqg_adam_loop_workspace_bytes.restype = c_sz
+    lib.sqg_adam_loop_workspace_bytes.argtypes = [vp, c_int]
+    lib.sqg_decompose_adam_loop.argtypes = [vp, vp, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double, c_int,
+                                            ctypes.c_double, c_int, c_int, c_ll, c_int, ctypes.c_double,
+                                            ctypes.c_uint64, vp, c_sz, vp]
     lib.sqg_decompose_batched.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double,
                                           c_int, c_int, c_int, c_int, ctypes.c_ulonglong, vp, c_sz, vp]
 
@@ -170,6 +175,7 @@ EXPORTED_SYMBOLS = [
     "sqg_cost_grad_checkpoint_workspace_bytes", "sqg_cost_grad", "sqg_cost_grad_noalloc", "sqg_apply_workspace_bytes",
     "sqg_apply",
     "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched", "sqg_decompose_batched_adam",
+    "sqg_adam_loop_workspace_bytes", "sqg_decompose_adam_loop",
     "sqg_state_workspace_bytes", "sqg_state_block_count", "sqg_apply_state",
     "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
     "sqg_mlp_gemm_bf16", "sqg_mlp_to_bf16", "sqg_mlp_relu_backward", "sqg_mlp_col_sum", "sqg_mlp_adam",

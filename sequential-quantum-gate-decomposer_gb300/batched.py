@@ -77,6 +77,41 @@ class BatchedDecomposer:
         return x, cost, calls
 
 
+def adam_decompose_graph(circuit, target_udag, x0, tolerance=1e-8, max_iters=100000, eta=1e-3, adaptive_eta=True,
+                         random_shift_count_max=100, randomization_threshold=2500000, max_outer=1,
+                         current_minimum=None, seed=0, trace_offset=0, cost_variant=0, workspace=None, stream=None):
+    """One decomposition of target_udag ((2**n, cols) complex128, U^dagger) with SQUANDER's ADAM
+    engine for any register the gradient supports, run on the device as a single CUDA graph
+    launch (sqg_decompose_adam_loop: a conditional while-node over [cost + gradient kernels,
+    one engine pass]), with no host round trip between evaluations.  Starts at x0 (P,) with
+    the running minimum current_minimum (None: a fresh decomposition).  Returns CUDA tensors
+    (x (P,) best point, cost (1,), evals (1,) int32, shifts (1,) int32); asynchronous on stream."""
+    dev.require_cuda()
+    native = circuit.native() if isinstance(circuit, Circuit) else circuit
+    t = dev.to_device_complex(target_udag)
+    if t.dim() != 2 or t.shape[0] != (1 << native.qbit_num):
+        raise ValueError("target must be (2**qbit_num, cols)")
+    x = dev.to_device_real(x0).reshape(-1).clone()
+    if x.numel() != native.param_num:
+        raise ValueError("x0 must hold %d parameters" % native.param_num)
+    cost = dev.torch.empty(1, dtype=dev.torch.float64, device="cuda")
+    evals = dev.torch.empty(1, dtype=dev.torch.int32, device="cuda")
+    shifts = dev.torch.empty(1, dtype=dev.torch.int32, device="cuda")
+    lib = _native.lib()
+    cols = int(t.shape[1])
+    ws = (workspace or dev.Workspace()).get(lib.sqg_adam_loop_workspace_bytes(native.handle, cols))
+    cur = np.finfo(np.float64).max if current_minimum is None or not np.isfinite(current_minimum) else current_minimum
+    _native.check(lib.sqg_decompose_adam_loop(
+        native.handle, dev.ptr(t), cols, int(trace_offset), int(cost_variant), dev.ptr(x), dev.ptr(cost),
+        dev.ptr(evals), dev.ptr(shifts), float(tolerance), int(max_iters), float(eta), 1 if adaptive_eta else 0,
+        int(random_shift_count_max), int(randomization_threshold), int(max_outer), float(cur),
+        int(seed) & 0xFFFFFFFFFFFFFFFF, dev.ptr(ws), ws.numel(), dev.stream_ptr(stream)), "sqg_decompose_adam_loop")
+    if stream is not None:  # the scratch and the target stay allocated until that stream is past the graph
+        ws.record_stream(stream)
+        t.record_stream(stream)
+    return x, cost, evals, shifts
+
+
 def random_start(B, P, rng):
     """RANDOM initial guess of Decomposition_Base (U[0, 2 pi), Decomposition_Base.cpp:415-436)."""
     return rng.uniform(0.0, 2 * np.pi, (B, P))

@@ -20,6 +20,7 @@
 #include "../../include/sqg.h"
 #include "gates.cuh"
 #include "handle.h"
+#include "adam.cuh"
 #include "tile.cuh"
 
 using namespace sqg;
@@ -487,27 +488,6 @@ __device__ __forceinline__ int block_allmax_int(int v, double* scratch) {
   return t;
 }
 
-// Sums of K per-thread values over the CTA, returned to every thread in a fixed order.
-// scratch: K * kTileMaxWarps doubles.
-template <int K>
-__device__ __forceinline__ void block_allsum_n(double (&v)[K], double* scratch) {
-#pragma unroll
-  for (int k = 0; k < K; k++)
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0)
-#pragma unroll
-    for (int k = 0; k < K; k++) scratch[k * kTileMaxWarps + warp] = v[k];
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < K; k++) {
-    double t = 0.0;
-    for (int w = 0; w < nw; w++) t += scratch[k * kTileMaxWarps + w];
-    v[k] = t;
-  }
-}
-
 // BFGS_Powell::BFGS_iteration (BFGS_Powell.cpp:202-396); returns the updated norm_Z.
 //
 // Z is held as Zs diag(cs): column scalings are recorded in cs and folded into the next
@@ -787,149 +767,24 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
   return f;
 }
 
-__device__ __forceinline__ unsigned long long splitmix_step(unsigned long long& s) {
-  s += 0x9E3779B97F4A7C15ULL;
-  unsigned long long z = s;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-  return z ^ (z >> 31);
-}
-__device__ __forceinline__ double splitmix_u01(unsigned long long& s) {
-  return (double)(splitmix_step(s) >> 11) * (1.0 / 9007199254740992.0);
-}
-
-// SQUANDER's ADAM engine for one target (Optimization_Interface::
-// solve_layer_optimization_problem_ADAM, optimization_engines/ADAM.cpp:44-330) with its Adam
-// optimizer (common/Adam.cpp: beta1 0.68, beta2 0.8, epsilon 1e-4; reset :70-100, update
-// :138-270) and randomize_parameters (decomposition/Optimization_Interface.cpp:576-607:
-// 30% of the parameters moved by U(-2 pi, 2 pi) * sqrt(f) around the best point).  The scalar
-// bookkeeping is replicated in every thread; thread 0 draws the random numbers from the
-// target's splitmix64 stream.  Adam's bias-correction powers advance once per parameter in
-// parameter order, as in the reference; pw1/pw2 hold beta^(i + 1).  Starts from sh.x, leaves
-// the best point in sh.bestx and returns the minimum.
+// SQUANDER's ADAM engine for one target (adam.cuh) with the evaluation of this kernel:
+// starts from sh.x, leaves the best point in sh.bestx and returns the minimum.  f0_vec and
+// dec_vec are the engine's 100- and 20-entry windows.
 template <int FORM>
 __device__ double dec_adam(const DecArgs& a, const Sh& sh, int b, int& calls, int& shifts, double cur_min,
                            unsigned long long& rng, double* f0_vec, int* dec_vec) {
-  const int P = a.P;
-  double *xt = sh.x, *g = sh.g, *best = sh.bestx, *mom = sh.v, *var = sh.vp, *pw1 = sh.S, *pw2 = sh.sdv;
-  const double b1 = 0.68, b2 = 0.8, aeps = 1e-4, kPi = 3.14159265358979323846;
-  if (threadIdx.x == 0) {
-    double t1 = 1.0, t2 = 1.0;
-    for (int i = 0; i < P; i++) {
-      t1 = t1 * b1;
-      t2 = t2 * b2;
-      pw1[i] = t1;
-      pw2[i] = t2;
-    }
-  }
-  double eta = a.eta;
-  double beta1_t = 1.0, beta2_t = 1.0, f0_mean = 0.0, dec_test = -1.0, f0_prev = DBL_MAX;
-  int f0_idx = 0, dec_idx = 0;
-  auto reset_arrays = [&]() {
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {
-      mom[i] = 0.0;
-      var[i] = 0.0;
-    }
-    for (int i = threadIdx.x; i < 100; i += blockDim.x) f0_vec[i] = 0.0;
-    for (int i = threadIdx.x; i < 20; i += blockDim.x) dec_vec[i] = -1;
-  };
-  reset_arrays();
-  for (int i = threadIdx.x; i < P; i += blockDim.x) best[i] = xt[i];
-  __syncthreads();
-  double hold = cur_min;
-  long long sub_iter = 0;
-  int status = 0, shift_cnt = 0;  // random_shift_count of this engine call
+  const AdamConfig cfg = {a.P, a.tol, a.eta, a.adaptive_eta, a.shift_max, a.rand_thr};
+  const AdamVecs v = {sh.x, sh.g, sh.bestx, sh.v, sh.vp, sh.S, sh.sdv, f0_vec, dec_vec, sh.redd};
+  adam_powers(v, a.P);
+  AdamRun s;
+  adam_begin(s, cfg, v, cur_min);
   for (int it = 0; it < a.max_calls; it++) {
-    const double f0 = dec_eval<FORM>(a, sh, xt, g, b);
+    const double f0 = dec_eval<FORM>(a, sh, sh.x, sh.g, b);
     calls++;
-    if (sub_iter == 1) {
-      hold = f0;
-      if (a.adaptive_eta) eta = eta > 1e-3 ? eta : 1e-3;
-    }
-    if (hold * 0.95 > f0 || (hold * 0.97 > f0 && f0 < 1e-3) || (hold * 0.99 > f0 && f0 < 1e-4)) {
-      sub_iter = 0;
-      hold = f0;
-    }
-    if (cur_min > f0) {
-      cur_min = f0;
-      for (int i = threadIdx.x; i < P; i += blockDim.x) best[i] = xt[i];
-      if (a.adaptive_eta) {  // the second clamp overwrites the first, as in the reference
-        const double ne = 1e-3 * f0;
-        eta = ne > 1e-6 ? ne : 1e-6;
-        eta = ne < 1e-1 ? ne : 1e-1;
-      }
-    }
-    if (f0 < a.tol || shift_cnt > a.shift_max) break;
-    if (sub_iter > a.rand_thr || status != 0) {
-      sub_iter = 0;
-      shift_cnt++;
-      hold = cur_min;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        const double r = sqrt(f0);
-        for (int j = 0; j < P; j++) {
-          if (splitmix_u01(rng) <= 0.3)
-            xt[j] = best[j] + (-2 * kPi + 4 * kPi * splitmix_u01(rng)) * r * 1.0;
-          else
-            xt[j] = best[j];
-        }
-      }
-      beta1_t = 1.0;
-      beta2_t = 1.0;
-      f0_mean = 0.0;
-      f0_idx = 0;
-      dec_idx = 0;
-      dec_test = -1.0;
-      f0_prev = DBL_MAX;
-      reset_arrays();
-      status = 0;
-      __syncthreads();
-    } else {
-      f0_mean = f0_mean + (f0 - f0_vec[f0_idx]) / 100;
-      int dv = dec_vec[dec_idx];
-      __syncthreads();  // every thread has read the entries rewritten below
-      if (threadIdx.x == 0) f0_vec[f0_idx] = f0;
-      f0_idx = (f0_idx + 1) % 100;
-      if (f0 < f0_prev) {
-        if (dv != 1) dec_test = dec_test + 2.0 / 20;
-        dv = 1;
-      } else {
-        if (dv == 1) dec_test = dec_test - 2.0 / 20;
-        dv = -1;
-      }
-      if (threadIdx.x == 0) dec_vec[dec_idx] = dv;
-      dec_idx = (dec_idx + 1) % 20;
-      f0_prev = f0;
-      double red[2] = {0.0, 0.0};
-      __syncthreads();  // the new window entry is visible below
-      for (int i = threadIdx.x; i < 100; i += blockDim.x) {
-        const double d = f0_vec[i] - f0_mean;
-        red[0] = fma(d, d, red[0]);
-      }
-      for (int i = threadIdx.x; i < P; i += blockDim.x) red[1] += var[i];
-      block_allsum_n(red, sh.redd);
-      const double var_f0 = sqrt(red[0]) / 100, grad_var = red[1];
-      const double eps = (grad_var < aeps && dec_test > 0.7) ? aeps / 100 : aeps;
-      for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        const double gi = g[i];
-        const double m = b1 * mom[i] + (1 - b1) * gi;
-        const double v = b2 * var[i] + (1 - b2) * gi * gi;
-        mom[i] = m;
-        var[i] = v;
-        const double mh = m / (1 - beta1_t * pw1[i]);
-        const double vh = v / (1 - beta2_t * pw2[i]);
-        xt[i] = xt[i] - eta * mh / (sqrt(vh) + eps);
-      }
-      beta1_t = beta1_t * pw1[P - 1];
-      beta2_t = beta2_t * pw2[P - 1];
-      status = (fabs(f0_mean - f0) < 1e-6 && dec_test <= 0.7 && var_f0 / f0_mean < 1e-6) ? 1 : 0;
-      __syncthreads();
-    }
-    sub_iter++;
+    if (adam_after_eval(s, cfg, v, f0, rng)) break;
   }
-  __syncthreads();
-  shifts += shift_cnt;
-  return cur_min;
+  shifts += s.shift_cnt;
+  return s.cur_min;
 }
 
 // Shared-memory layout common to the decomposition and evaluation kernels (dec_smem_bytes

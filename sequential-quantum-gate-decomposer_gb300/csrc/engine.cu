@@ -240,7 +240,18 @@ int choose_threads(int tc, int N, bool grad) {
   return t;
 }
 
-TilePlan plan_tiles(int N, int cols, bool grad) {
+int device_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 1;
+  return std::max(sms, 1);
+}
+
+// Column tiles of a launch over B instances of `cols` columns.  A tile holds as many columns
+// as the shared-memory budget takes (a power of two); when the whole launch would then not
+// give every SM two CTAs (small batches: a single decomposition's evaluation), tiles are
+// narrowed down to one column each, so the FP64 work of one instance spreads over the GPU.
+TilePlan plan_tiles(int N, int cols, bool grad, int B = 0) {
   const size_t per = (size_t)N * sizeof(double2) * (grad ? 2 : 1);
   size_t budget = grad ? kSmemBudgetGrad : kSmemBudgetFwd;
   int tc = (int)std::max<size_t>(1, budget / per);
@@ -248,6 +259,10 @@ TilePlan plan_tiles(int N, int cols, bool grad) {
   int p2 = 1;
   while (p2 * 2 <= tc) p2 *= 2;
   tc = std::min(p2, cols);
+  if (B > 0) {
+    const long long want = 2LL * device_sms();
+    while (tc > 1 && (long long)B * ((cols + tc - 1) / tc) < want) tc >>= 1;
+  }
   TilePlan pl;
   pl.TC = tc;
   pl.tiles = (cols + tc - 1) / tc;
@@ -294,7 +309,7 @@ struct EvalLayout {
 EvalLayout eval_layout(const sqg_circuit* c, int B, int cols, bool grad, int ckpt_interval) {
   EvalLayout l;
   l.prep = prep_layout(c, B, 0);
-  l.plan = plan_tiles(c->N, cols, grad);
+  l.plan = plan_tiles(c->N, cols, grad, B);
   l.tr_off = l.prep.end;
   l.gr_off = align_up(l.tr_off + (size_t)B * l.plan.tiles * sizeof(double2), 256);
   size_t gr_bytes = grad ? (size_t)B * l.plan.tiles * std::max(c->P, 1) * sizeof(double2) : 0;

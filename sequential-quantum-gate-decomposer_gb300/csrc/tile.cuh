@@ -86,6 +86,27 @@ __device__ __forceinline__ double block_allsum(double v, double* scratch) {
   return t;
 }
 
+// Sums of K per-thread values over the CTA, returned to every thread in a fixed order.
+// scratch: K * kTileMaxWarps doubles.
+template <int K>
+__device__ __forceinline__ void block_allsum_n(double (&v)[K], double* scratch) {
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) scratch[k * kTileMaxWarps + warp] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double t = 0.0;
+    for (int w = 0; w < nw; w++) t += scratch[k * kTileMaxWarps + w];
+    v[k] = t;
+  }
+}
+
 __device__ __forceinline__ double block_allmin(double v, double* scratch) {
   for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
   const int nw = blockDim.x >> 5;

@@ -14,8 +14,10 @@ import math
 import numpy as np
 
 from . import _device as dev
+from . import _native
 from .circuit import Circuit, combined_unitary_device
 from .evaluator import FROBENIUS_NORM, SUPPORTED_VARIANTS, CostEvaluator
+from .batched import BatchedDecomposer, adam_decompose_graph
 from .optim import adam_squander, bfgs_powell
 
 _GUESS = {"zeros": "ZEROS", "random": "RANDOM", "close_to_zero": "CLOSE_TO_ZERO"}
@@ -55,6 +57,10 @@ class N_Qubit_Decomposition_custom:
         self.decomposition_error = None
         self.num_iters = 0
         self._evaluator = None
+        self._loop_ws = dev.Workspace()
+        # True: drive every evaluation from the host (optim.py), the form the device loops are
+        # tested against
+        self._host_loops = False
 
     # ---- configuration -----------------------------------------------------------------
     def set_Gate_Structure(self, gate_structure):
@@ -311,10 +317,34 @@ class N_Qubit_Decomposition_custom:
         x = self.rng.uniform(0.0, 2 * math.pi, P)
         return x / 100 if self.initial_guess == "CLOSE_TO_ZERO" else x
 
+    def _bfgs_on_device(self, target, guess, tol, max_inner, loops):
+        """iteration_loops BFGS runs of one outer iteration in one k_decompose launch (batch 1).
+        Returns (minimum, evaluations, best point), or None (and switches to host-driven BFGS)
+        when the gate structure does not fit one CTA."""
+        dec = BatchedDecomposer(self.circuit, tolerance=tol, max_calls=max_inner, max_outer=1,
+                                iteration_loops=loops, stop_at_tolerance=False, trace_offset=self.trace_offset,
+                                cost_variant=self.cost_variant)
+        try:
+            xd, cd, ed = dec.run(target.unsqueeze(0), guess.reshape(1, -1), seed=int(self.rng.integers(1 << 62)))
+        except _native.SQGError as e:
+            if "unsupported" not in str(e):
+                raise
+            self._host_loops = True
+            return None
+        return float(cd.item()), int(ed.item()), xd.reshape(-1).cpu().numpy()
+
     def Start_Decomposition(self):
         """Decomposition_Base::solve_optimization_problem for the custom structure
         (Decomposition_Base.cpp:375-700 with optimization_block = all gates) with the
-        BFGS restarts of optimization_engines/BFGS.cpp:121-150."""
+        BFGS restarts of optimization_engines/BFGS.cpp:121-150 or the ADAM engine of
+        optimization_engines/ADAM.cpp:44-330.
+
+        Every outer iteration runs on the device without a host round trip per evaluation:
+        ADAM as one CUDA graph launch (batched.adam_decompose_graph), BFGS up to five qubits
+        as one k_decompose launch of iteration_loops runs.  BFGS above five qubits drives
+        the device cost and gradient from the host (optim.bfgs_powell).  The outer loop and
+        its tolerance test stay on the host, so each launch is bounded by one outer
+        iteration's evaluation budget."""
         P = self.get_Parameter_Num()
         if P == 0:
             self.optimized_parameters = np.zeros(0)
@@ -328,6 +358,7 @@ class N_Qubit_Decomposition_custom:
         loops = int(self.config.get("max_iteration_loops", 3 if self.qbit_num == 2 else 1))
         guess = self._initial(P)
         best_x, best_f = guess.copy(), math.inf
+        target = self.evaluator().target
         for _outer in range(max_outer):
             if self.optimizer == "ADAM":
                 # solve_layer_optimization_problem_ADAM (optimization_engines/ADAM.cpp:44-330); the
@@ -338,20 +369,36 @@ class N_Qubit_Decomposition_custom:
                 adaptive = bool(cfg["adaptive_eta"]) if "adaptive_eta" in cfg else True
                 thr = int(cfg.get("randomization_threshold_adam", cfg.get("randomization_threshold", 2500000)))
                 tol_a = float(cfg.get("optimization_tolerance_adam", tol))
-                x = guess.copy()
-                f, calls = adam_squander(self._fg, x, max_inner, tol_a, eta, adaptive,
-                                         int(cfg.get("random_shift_count_max", self.random_shift_count_max)), thr,
-                                         seed=int(self.rng.integers(1 << 62)), current_minimum=best_f)
+                shift_max = int(cfg.get("random_shift_count_max", self.random_shift_count_max))
+                seed = int(self.rng.integers(1 << 62))
+                if self._host_loops:
+                    x = guess.copy()
+                    f, calls = adam_squander(self._fg, x, max_inner, tol_a, eta, adaptive, shift_max, thr,
+                                             seed=seed, current_minimum=best_f)
+                else:
+                    xd, cd, ed, _sd = adam_decompose_graph(
+                        self.circuit, target, guess, tol_a, max_inner, eta, adaptive, shift_max, thr, max_outer=1,
+                        current_minimum=best_f, seed=seed, trace_offset=self.trace_offset,
+                        cost_variant=self.cost_variant, workspace=self._loop_ws)
+                    f, calls, x = float(cd.item()), int(ed.item()), xd.cpu().numpy()
                 self.num_iters += calls
                 if f < best_f:
                     best_f, best_x = f, x.copy()
             else:
-                for _loop in range(loops):
-                    f, calls = bfgs_powell(self._fg, guess, max_inner)
-                    self.num_iters += calls
-                    if f < best_f:
-                        best_f, best_x = f, guess.copy()
-                        guess += self.rng.uniform(0.0, 2 * math.pi, P) / 100
+                if self.qbit_num <= 5 and not self._host_loops:
+                    run = self._bfgs_on_device(target, guess, tol, max_inner, loops)
+                    if run is not None:
+                        f, calls, x = run
+                        self.num_iters += calls
+                        if f < best_f:
+                            best_f, best_x = f, x
+                if self.qbit_num > 5 or self._host_loops:
+                    for _loop in range(loops):
+                        f, calls = bfgs_powell(self._fg, guess, max_inner)
+                        self.num_iters += calls
+                        if f < best_f:
+                            best_f, best_x = f, guess.copy()
+                            guess += self.rng.uniform(0.0, 2 * math.pi, P) / 100
             guess = best_x.copy()
             if abs(best_f) < tol:
                 break
