@@ -17,7 +17,8 @@
  * device memory.  Calls are asynchronous on the given CUDA stream
  * (cudaStream_t passed as void*, NULL = legacy default stream) and return a status
  * code; no C++ exception crosses this boundary.  A circuit handle is immutable after
- * creation and may be used from several threads and streams at once.
+ * creation (apart from sqg_circuit_set_partitions, which replaces its state-vector plan)
+ * and may be used from several threads and streams at once.
  */
 #ifndef SQG_H
 #define SQG_H
@@ -172,6 +173,16 @@ int sqg_apply(const sqg_circuit* circuit, const double* theta_dev, int batch, vo
  * 13 qubits are accepted only by this entry point.  Workspace: sqg_state_workspace_bytes. */
 size_t sqg_state_workspace_bytes(const sqg_circuit* circuit, int batch);
 int sqg_state_block_count(const sqg_circuit* circuit);
+
+/* Hands a partitioning of the gate list to the fused state-vector plan: part_ends[i] is the
+ * gate index after partition i (non-decreasing, the last equal to gate_num).  Fused passes
+ * then start only at partition boundaries, consecutive partitions merged while their qubits
+ * with the five lowest number at most 12 (a partition larger than that is split gate by gate);
+ * nparts == 0 restores the gate-by-gate plan.  The partitions come from the partitioner
+ * (squander/partitioning/partition.py:PartitionCircuit, kahn.py), which reorders the gates so
+ * that each partition spans few qubits.  Rebuilds the plan synchronously; no work that uses
+ * the circuit may be in flight. */
+int sqg_circuit_set_partitions(sqg_circuit* circuit, const int* part_ends, int nparts);
 int sqg_apply_state(const sqg_circuit* circuit, const double* theta_dev, int batch, void* states_dev,
                     long long state_stride, int fused, void* workspace_dev, size_t workspace_bytes, void* stream);
 

@@ -123,6 +123,7 @@ def _declare(lib):
     lib.sqg_state_workspace_bytes.restype = c_sz
     lib.sqg_state_workspace_bytes.argtypes = [vp, c_int]
     lib.sqg_state_block_count.argtypes = [vp]
+    lib.sqg_circuit_set_partitions.argtypes = [vp, vp, c_int]
     lib.sqg_apply_state.argtypes = [vp, vp, c_int, vp, c_ll, c_int, vp, c_sz, vp]
     lib.sqg_decompose_batched_adam.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double,
                                                c_int, ctypes.c_double, c_int, c_int, c_ll, c_int, ctypes.c_uint64, vp]
@@ -176,7 +177,7 @@ EXPORTED_SYMBOLS = [
     "sqg_apply",
     "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched", "sqg_decompose_batched_adam",
     "sqg_adam_loop_workspace_bytes", "sqg_decompose_adam_loop",
-    "sqg_state_workspace_bytes", "sqg_state_block_count", "sqg_apply_state",
+    "sqg_state_workspace_bytes", "sqg_state_block_count", "sqg_apply_state", "sqg_circuit_set_partitions",
     "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
     "sqg_mlp_gemm_bf16", "sqg_mlp_to_bf16", "sqg_mlp_relu_backward", "sqg_mlp_col_sum", "sqg_mlp_adam",
     "sqg_mlp_angle_head", "sqg_mlp_features",

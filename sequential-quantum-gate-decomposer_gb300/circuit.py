@@ -44,17 +44,73 @@ class NativeCircuit:
             self.handle = None
 
 
+class Gate:
+    """One gate of a Circuit (the gate objects of squander's gates_Wrapper): type, target,
+    control (-1 when uncontrolled) and the start index of its parameters in the circuit that
+    holds it.  Also reads as the gate dictionary of the decomposition classes' get_Gates
+    ("type", "target_qbit", "control_qbit", "parameter_start_index")."""
+
+    def __init__(self, gtype, target, control, param_start, index=-1):
+        self.type, self.target, self.control = int(gtype), int(target), int(control)
+        self.param_start = int(param_start)
+        self._index = int(index)  # position among the top-level items of its circuit
+
+    def get_Name(self):
+        return GATE_NAMES[self.type]
+
+    def get_Target_Qbit(self):
+        return self.target
+
+    def get_Control_Qbit(self):
+        return self.control
+
+    def get_Involved_Qbits(self):
+        return sorted((self.target, self.control)) if self.control >= 0 else [self.target]
+
+    def get_Parameter_Num(self):
+        return PARAM_NUM[self.type]
+
+    def get_Parameter_Start_Index(self):
+        return self.param_start
+
+    def _as_dict(self):
+        d = {"type": GATE_NAMES[self.type], "target_qbit": self.target, "parameter_start_index": self.param_start}
+        if self.control >= 0:
+            d["control_qbit"] = self.control
+        return d
+
+    def __getitem__(self, key):
+        return self._as_dict()[key]
+
+    def __contains__(self, key):
+        return key in self._as_dict()
+
+    def get(self, key, default=None):
+        return self._as_dict().get(key, default)
+
+    def keys(self):
+        return self._as_dict().keys()
+
+    def __repr__(self):
+        return "Gate(%s)" % self._as_dict()
+
+
 class Circuit:
-    """Ordered parametric gate list on ``qbit_num`` qubits (SQUANDER ``qgd_Circuit``)."""
+    """Ordered parametric gate list on ``qbit_num`` qubits (SQUANDER ``qgd_Circuit``), with
+    nested sub-circuits (add_Circuit) kept as blocks of the top-level item list; the engine
+    sees the flattened gate list."""
 
     def __init__(self, qbit_num):
         if int(qbit_num) < 1:
             raise ValueError("qbit_num must be positive")
         self.qbit_num = int(qbit_num)
-        self._gates = []  # (type, target, control)
+        self._gates = []  # flattened (type, target, control)
+        self._items = []  # top level: ("g", flat index) or ("c", sub-circuit, first flat index)
         self._native = None
         self._ws = dev.Workspace()
         self.min_fusion = -1
+        self._pstart = 0  # parameter start index inside the circuit that holds this one
+        self._index = -1
 
     # ---- structure -------------------------------------------------------------------
     def _check_qubit(self, q, what):
@@ -67,6 +123,7 @@ class Circuit:
             self._check_qubit(control, "control")
             if control == target:
                 raise ValueError("control and target qubits must differ")
+        self._items.append(("g", len(self._gates)))
         self._gates.append((gtype, int(target), int(control)))
         self._native = None
 
@@ -92,12 +149,46 @@ class Circuit:
         self._add(CRY, target_qbit, control_qbit)
 
     def add_Circuit(self, other):
-        """Append a sub-circuit; its gates are flattened in order (SQUANDER keeps a
-        nested block whose parameters are likewise contiguous)."""
+        """Append a sub-circuit as one block (Gates_block::add_gate of a nested block, its
+        parameters contiguous after the ones before it)."""
         if other.qbit_num > self.qbit_num:
             raise ValueError("sub-circuit spans more qubits than the circuit")
+        sub = other._copy()
+        self._items.append(("c", sub, len(self._gates)))
         self._gates.extend(other._gates)
         self._native = None
+
+    def add_Gate(self, gate):
+        """Append a copy of a gate object taken from another circuit's get_Gates (a sub-circuit
+        object is appended as a block)."""
+        if isinstance(gate, Circuit):
+            self.add_Circuit(gate)
+        else:
+            self._add(gate.type, gate.target, gate.control)
+
+    def _copy(self):
+        c = Circuit(self.qbit_num)
+        c._gates = list(self._gates)
+        c._items = [(it[0], it[1]._copy(), it[2]) if it[0] == "c" else it for it in self._items]
+        c.min_fusion = self.min_fusion
+        return c
+
+    def _item_ranges(self):
+        """(first flat gate, end flat gate) of every top-level item."""
+        out = []
+        for it in self._items:
+            if it[0] == "g":
+                out.append((it[1], it[1] + 1))
+            else:
+                out.append((it[2], it[2] + len(it[1]._gates)))
+        return out
+
+    def block_ends(self):
+        """Flat gate index after every top-level item that is a block (sub-circuit); empty
+        for a circuit without blocks."""
+        if not any(it[0] == "c" for it in self._items):
+            return []
+        return [e for (_, e) in self._item_ranges()]
 
     def get_Qbit_Num(self):
         return self.qbit_num
@@ -109,14 +200,32 @@ class Circuit:
         return len(self._gates)
 
     def get_Gates(self):
+        """Top-level gates (Gate objects) and sub-circuits, each with its parameter start index
+        in this circuit (qgd_Circuit.get_Gates)."""
         out, p = [], 0
-        for t, tg, c in self._gates:
-            d = {"type": GATE_NAMES[t], "target_qbit": tg, "parameter_start_index": p}
-            if c >= 0:
-                d["control_qbit"] = c
-            out.append(d)
+        for k, it in enumerate(self._items):
+            if it[0] == "g":
+                t, tg, c = self._gates[it[1]]
+                out.append(Gate(t, tg, c, p, k))
+                p += PARAM_NUM[t]
+            else:
+                sub = it[1]
+                sub._pstart, sub._index = p, k
+                out.append(sub)
+                p += sub.get_Parameter_Num()
+        return out
+
+    def get_Flat_Gates(self):
+        """Every gate of the flattened circuit (Gate objects, parameter start index in this
+        circuit)."""
+        out, p = [], 0
+        for k, (t, tg, c) in enumerate(self._gates):
+            out.append(Gate(t, tg, c, p, k))
             p += PARAM_NUM[t]
         return out
+
+    def get_Involved_Qbits(self):
+        return self.get_Qbits()
 
     def Remap_Qbits(self, qbit_map, qbit_num=None):
         """New circuit with qubit q of every gate moved to qbit_map[q] (a dict {initial:
@@ -125,7 +234,11 @@ class Circuit:
         n = self.qbit_num if qbit_num is None else int(qbit_num)
         m = dict(qbit_map) if isinstance(qbit_map, dict) else {q: int(v) for q, v in enumerate(qbit_map)}
         out = Circuit(n)
-        for t, tg, c in self._gates:
+        for it in self._items:
+            if it[0] == "c":
+                out.add_Circuit(it[1].Remap_Qbits(m, n))
+                continue
+            t, tg, c = self._gates[it[1]]
             if tg not in m or (c >= 0 and c not in m):
                 raise ValueError("qbit_map does not cover every qubit of the circuit")
             out._add(t, int(m[tg]), int(m[c]) if c >= 0 else -1)
@@ -136,11 +249,23 @@ class Circuit:
         return sorted({q for _, tg, c in self._gates for q in ((tg, c) if c >= 0 else (tg,))})
 
     def _gate_qubits(self, k):
-        _, tg, c = self._gates[k]
+        """Qubits of top-level item k (a sub-circuit: all qubits of its gates)."""
+        it = self._items[k]
+        if it[0] == "c":
+            return tuple(it[1].get_Qbits())
+        _, tg, c = self._gates[it[1]]
         return (tg, c) if c >= 0 else (tg,)
 
+    def _item_index(self, gate):
+        k = gate if isinstance(gate, (int, np.integer)) else getattr(gate, "_index", -1)
+        if not 0 <= k < len(self._items):
+            raise ValueError("the gate is not a top-level item of this circuit")
+        return int(k)
+
     def get_Parents(self, gate):
-        """Indices of the gates that last act, before gate `gate`, on each of its qubits."""
+        """Indices of the top-level items that last act, before `gate` (an index or an object
+        from get_Gates), on each of its qubits (Gates_block::determine_parents)."""
+        gate = self._item_index(gate)
         out = set()
         for q in self._gate_qubits(gate):
             for k in range(gate - 1, -1, -1):
@@ -150,10 +275,12 @@ class Circuit:
         return sorted(out)
 
     def get_Children(self, gate):
-        """Indices of the gates that next act, after gate `gate`, on each of its qubits."""
+        """Indices of the top-level items that next act, after `gate`, on each of its qubits
+        (Gates_block::determine_children)."""
+        gate = self._item_index(gate)
         out = set()
         for q in self._gate_qubits(gate):
-            for k in range(gate + 1, len(self._gates)):
+            for k in range(gate + 1, len(self._items)):
                 if q in self._gate_qubits(k):
                     out.add(k)
                     break
@@ -166,7 +293,7 @@ class Circuit:
         return nums
 
     def get_Parameter_Start_Index(self):
-        return 0
+        return self._pstart
 
     def set_min_fusion(self, min_fusion):
         """Recorded for API compatibility: the engine always applies the whole circuit to
@@ -182,8 +309,16 @@ class Circuit:
         return np.asarray(recs, dtype=np.int32).reshape(-1, 4)
 
     def native(self):
+        """The engine's handle of the flattened circuit; a circuit of blocks (a partitioned
+        circuit) also hands its block boundaries to the fused state-vector plan."""
         if self._native is None:
-            self._native = NativeCircuit(self.qbit_num, self.gate_records())
+            nc = NativeCircuit(self.qbit_num, self.gate_records())
+            ends = self.block_ends()
+            if ends:
+                arr = np.ascontiguousarray(ends, dtype=np.int32)
+                _native.check(_native.lib().sqg_circuit_set_partitions(nc.handle, arr.ctypes.data, arr.size),
+                              "sqg_circuit_set_partitions")
+            self._native = nc
         return self._native
 
     # ---- device-level operations (torch CUDA tensors in, results in place) -----------

@@ -350,11 +350,13 @@ constexpr int kStateLow = 5;       // the lowest qubits belong to every chunk (5
 constexpr int kStateThreads = 256;
 
 // Groups the gates into blocks: a block grows while the qubits it touches, together with the
-// lowest kStateLow ones, number at most K; each block is one pass over the state.  Fills the
-// chunk with further qubits (lowest first), maps every gate of the block to chunk-local qubit
-// positions and tabulates the global offsets of the chunk's high local bits and the qubits
-// that number the chunks.
-int build_state_plan(sqg_circuit* c) {
+// lowest kStateLow ones, number at most K; each block is one pass over the state.  With
+// partition ends (`cuts`, the gate index after each partition) a block grows by whole
+// partitions and breaks only between them, unless one partition alone exceeds the chunk (it
+// is then split gate by gate).  Fills the chunk with further qubits (lowest first), maps every
+// gate of the block to chunk-local qubit positions and tabulates the global offsets of the
+// chunk's high local bits and the qubits that number the chunks.
+int build_state_plan(sqg_circuit* c, const std::vector<int>& cuts = {}) {
   const int n = c->n, K = std::min(n, kStateK), low = std::min(K, kStateLow);
   c->sK = K;
   std::vector<Gate> lg(c->h_gates);
@@ -395,7 +397,7 @@ int build_state_plan(sqg_circuit* c) {
     std::fill(inA.begin(), inA.end(), 0);
   };
   int g0 = 0, used = 0;
-  for (int g = 0; g < c->L; g++) {
+  auto take_gate = [&](int g) {  // gate by gate: break wherever the chunk would overflow
     const Gate& gt = c->h_gates[g];
     int add = 0;
     int qs[2] = {gt.target, gate_controlled(gt.type) ? gt.control : -1};
@@ -411,6 +413,42 @@ int build_state_plan(sqg_circuit* c) {
         inA[q] = 1;
         used++;
       }
+  };
+  if (cuts.empty()) {
+    for (int g = 0; g < c->L; g++) take_gate(g);
+  } else {
+    std::vector<int> mark(n, 0);
+    int s0 = 0;
+    for (int e : cuts) {  // partition [s0, e)
+      std::vector<int> fresh;
+      for (int g = s0; g < e; g++) {
+        const Gate& gt = c->h_gates[g];
+        int qs[2] = {gt.target, gate_controlled(gt.type) ? gt.control : -1};
+        for (int q : qs)
+          if (q >= low && !mark[q]) {
+            mark[q] = 1;
+            fresh.push_back(q);
+          }
+      }
+      int add = 0, own = (int)fresh.size();
+      for (int q : fresh) {
+        if (!inA[q]) add++;
+        mark[q] = 0;
+      }
+      if (low + own > K) {  // the partition alone exceeds the chunk
+        for (int g = s0; g < e; g++) take_gate(g);
+      } else {
+        if (low + used + add > K) {
+          close_block(g0, s0);
+          g0 = s0;
+          used = 0;
+          add = own;
+        }
+        for (int q : fresh) inA[q] = 1;
+        used += add;
+      }
+      s0 = e;
+    }
   }
   if (c->L > 0) close_block(g0, c->L);
   if (c->L == 0) return SQG_OK;
@@ -536,6 +574,27 @@ int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_ci
   }
   *out = c;
   return SQG_OK;
+}
+
+int sqg_circuit_set_partitions(sqg_circuit* c, const int* part_ends, int nparts) {
+  if (!c) return fail(SQG_ERR_INVALID_ARGUMENT, "null circuit handle");
+  if (nparts < 0 || (nparts > 0 && !part_ends)) return fail(SQG_ERR_INVALID_ARGUMENT, "bad partition list");
+  std::vector<int> cuts(part_ends, part_ends + nparts);
+  for (int i = 0; i < nparts; i++)
+    if (cuts[i] < (i ? cuts[i - 1] : 0) || cuts[i] > c->L)
+      return fail(SQG_ERR_INVALID_ARGUMENT, "partition ends must be non-decreasing gate indices <= gate_num");
+  if (nparts > 0 && cuts.back() != c->L) return fail(SQG_ERR_INVALID_ARGUMENT, "the last partition must end at gate_num");
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != c->device) return fail(SQG_ERR_INVALID_ARGUMENT, "circuit handle belongs to another device");
+  cudaFree(c->d_lgates);
+  cudaFree(c->d_hitab);
+  cudaFree(c->d_inact);
+  c->d_lgates = nullptr;
+  c->d_hitab = nullptr;
+  c->d_inact = nullptr;
+  c->sblocks.clear();
+  return build_state_plan(c, cuts);
 }
 
 int sqg_circuit_destroy(sqg_circuit* c) {

@@ -171,7 +171,7 @@ class N_Qubit_Decomposition_custom:
         "target_qbit", "control_qbit", U3 "Theta"/"Phi"/"Lambda", RX/RY/CRY "Theta", RZ "Phi")."""
         out = []
         params = self.optimized_parameters
-        for d in self.circuit.get_Gates():
+        for d in self.circuit.get_Flat_Gates():
             g = {"type": d["type"], "target_qbit": d["target_qbit"]}
             if "control_qbit" in d:
                 g["control_qbit"] = d["control_qbit"]

@@ -82,3 +82,21 @@ def test_qc_sim_circuit_large_state(sqg, wl, n):
     assert abs(float(torch.linalg.vector_norm(a)) - 1.0) < 1e-12
     assert float((a - b).abs().max()) < 1e-12
     assert c.state_block_count() < c.get_Gate_Num() / 4
+
+
+@pytest.mark.parametrize("n,gates,mq", [(14, 400, 4), (16, 300, 7), (12, 300, 3)])
+def test_partitioned_circuit_state_matches_oracle(sqg, wl, n, gates, mq):
+    """A Kahn-partitioned circuit (PartitionCircuit) applied with fused passes that break only
+    at partition boundaries gives the original circuit's state."""
+    part = importlib.import_module("sequential-quantum-gate-decomposer_gb300.partitioning")
+    rng = np.random.default_rng(200 + n)
+    c = wl.all_gates_circuit(n, gates, rng)
+    p = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    pc, pp, parts = part.PartitionCircuit(c, p, mq)
+    psi = random_state(n, rng)
+    ref = O.apply_to(n, c.gate_records(), p, psi.reshape(-1, 1).copy()).reshape(-1)
+    d = torch.from_numpy(psi.copy()).cuda()
+    pc.apply_state_device(torch.from_numpy(pp).cuda(), d)
+    torch.cuda.synchronize()
+    assert float(np.abs(d.cpu().numpy() - ref).max()) < 1e-12
+    assert 1 <= pc.state_block_count() <= len(parts)
