@@ -218,6 +218,23 @@ int sqg_decompose_batched(const sqg_circuit* circuit, const void* targets_dev, i
                           int max_calls, int max_outer, int iteration_loops, int stop_at_tolerance,
                           unsigned long long seed, void* workspace_dev, size_t workspace_bytes, void* stream);
 
+/* Batched BFGS decompositions of many gate STRUCTURES at once (the inner loop of the
+ * structure-search decomposers, N_Qubit_Decomposition_Tree_Search::
+ * tree_search_over_gate_structures, src-cpp/decomposition/N_Qubit_Decomposition_Tree_Search.cpp:
+ * 1269-1451, which runs one N_Qubit_Decomposition_custom per candidate structure): instance b
+ * decomposes with its own gate list gates[b * gate_num .. (b + 1) * gate_num) (HOST array of
+ * batch x gate_num records).  Every list repeats the gate types and parameter layout of
+ * `circuit`; only target and control qubits may differ (checked, then copied to the
+ * workspace).  targets_dev + b * target_stride is instance b's target (target_stride 0: one
+ * shared target).  Otherwise as sqg_decompose_batched.  Workspace (256-byte aligned):
+ * sqg_decompose_structures_workspace_bytes. */
+size_t sqg_decompose_structures_workspace_bytes(const sqg_circuit* circuit, int batch, int cols);
+int sqg_decompose_structures(const sqg_circuit* circuit, const sqg_gate* gates, const void* targets_dev,
+                             long long target_stride, int cols, int batch, int trace_offset, int cost_variant,
+                             double* x_dev, double* cost_dev, int* calls_dev, int* iters_dev, double tolerance,
+                             int max_calls, int max_outer, int iteration_loops, int stop_at_tolerance,
+                             unsigned long long seed, void* workspace_dev, size_t workspace_bytes, void* stream);
+
 /* Batched decompositions with SQUANDER's ADAM engine: replaces
  * Optimization_Interface::solve_layer_optimization_problem_ADAM
  * (src-cpp/optimization_engines/ADAM.cpp:44-330) with its Adam optimizer

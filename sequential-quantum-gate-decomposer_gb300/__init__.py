@@ -4,7 +4,8 @@ The cost ``1 - Re Tr(C(theta) U^dagger)/cols`` (and the HILBERT_SCHMIDT_TEST /
 INFIDELITY variants) of a parametric U3/RX/RY/RZ/CNOT/CZ/CRY circuit and its adjoint
 gradient run in hand-written sm_103a CUDA kernels (libsqg.so, C ABI in include/sqg.h).
 This package mirrors the reference's Python surface for that path:
-``Circuit`` (squander.Circuit) and ``N_Qubit_Decomposition_custom``.
+``Circuit`` (squander.Circuit), ``N_Qubit_Decomposition_custom``,
+``N_Qubit_Decomposition_Tree_Search`` and ``PartitionCircuit`` (squander.partitioning).
 
 The directory name contains hyphens, so import it with
 ``importlib.import_module("sequential-quantum-gate-decomposer_gb300")``; the package
@@ -18,9 +19,12 @@ from .circuit import CNOT, CRY, CZ, RX, RY, RZ, U3, Circuit
 from .decomposition import N_Qubit_Decomposition_custom
 from .evaluator import (FROBENIUS_NORM, HILBERT_SCHMIDT_TEST, INFIDELITY, CircuitCost, CostEvaluator,
                         circuit_cost)
+from .partitioning import PartitionCircuit
+from .tree_search import N_Qubit_Decomposition_Tree_Search
 
 _sys.modules.setdefault("sqg_gb300", _sys.modules[__name__])
 
-__all__ = ["Circuit", "BatchedDecomposer", "N_Qubit_Decomposition_custom", "CostEvaluator", "CircuitCost", "circuit_cost", "SQGError",
+__all__ = ["Circuit", "BatchedDecomposer", "N_Qubit_Decomposition_custom", "N_Qubit_Decomposition_Tree_Search",
+           "PartitionCircuit", "CostEvaluator", "CircuitCost", "circuit_cost", "SQGError",
            "build", "FROBENIUS_NORM", "HILBERT_SCHMIDT_TEST", "INFIDELITY", "U3", "RX", "RY", "RZ", "CNOT", "CZ",
            "CRY"]

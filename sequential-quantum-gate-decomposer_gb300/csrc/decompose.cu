@@ -36,6 +36,7 @@ constexpr double kTwoPi = 6.283185307179586476925286766559;
 
 struct DecArgs {
   const Gate* gates;
+  long long gstride;  // gate records between the lists of consecutive instances (0: one shared list)
   int L, P, n, N, cols, trace_offset, variant;
   const double2* targets;
   long long tstride;
@@ -807,8 +808,9 @@ __device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
   sh.pgate = (int*)take(sizeof(int) * max(P, 1));
   sh.pg = (int*)take(sizeof(int) * max(L, 1));
   sh.npg = 0;
+  const Gate* gl = a.gates + (long long)b * a.gstride;  // this instance's gate list
   for (int g = 0; g < L; g++)
-    if (gate_param_num(a.gates[g].type) > 0) {
+    if (gate_param_num(gl[g].type) > 0) {
       if (threadIdx.x == 0) sh.pg[sh.npg] = g;
       sh.npg++;
     }
@@ -822,7 +824,7 @@ __device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
   sh.Z = nullptr;
   for (int e = threadIdx.x; e < NC; e += blockDim.x) tsh[e] = a.targets[(long long)b * a.tstride + e];
   for (int g = threadIdx.x; g < L; g += blockDim.x) {
-    const Gate gt = a.gates[g];
+    const Gate gt = gl[g];
     gsh[g] = gt;
     for (int k = 0; k < gate_param_num(gt.type); k++) sh.pgate[gt.pstart + k] = g;
   }
@@ -1121,6 +1123,79 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   return dec_launch<kBfgs>(c, a, batch, smem, stream);
 }
 
+
+size_t sqg_decompose_structures_workspace_bytes(const sqg_circuit* c, int batch, int cols) {
+  if (!c || batch <= 0 || cols <= 0) return 0;
+  const size_t z = z_in_shared(c, cols) ? 0 : (size_t)batch * c->P * c->P * sizeof(double);
+  return (z + 255) / 256 * 256 + (size_t)batch * std::max(c->L, 1) * sizeof(Gate) + 256;
+}
+
+int sqg_decompose_structures(const sqg_circuit* c, const sqg_gate* gates, const void* targets,
+                             long long target_stride, int cols, int batch, int trace_offset, int cost_variant,
+                             double* x, double* cost, int* calls, int* iters, double tolerance, int max_calls,
+                             int max_outer, int iteration_loops, int stop_at_tolerance, unsigned long long seed,
+                             void* workspace, size_t ws_bytes, void* stream) {
+  if (!c || !gates || !targets || !x || !cost || !calls || batch <= 0 || batch > 0x7fffffff / 2 || cols <= 0 ||
+      cols > c->N)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "bad circuit, gate lists, batch, targets or outputs");
+  if (c->P == 0) return set_error(SQG_ERR_INVALID_ARGUMENT, "the circuit has no free parameters");
+  if (cost_variant != SQG_FROBENIUS_NORM && cost_variant != SQG_HILBERT_SCHMIDT_TEST && cost_variant != SQG_INFIDELITY)
+    return set_error(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
+  const int off = cost_variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
+  if (off < 0 || off + cols > c->N) return set_error(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
+  if (c->n > 5) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 5");
+  if (max_calls < 1 || max_outer < 1 || iteration_loops < 1)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
+  if (target_stride != 0 && target_stride < (long long)c->N * cols)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "target stride must be 0 (one shared target) or at least rows * cols");
+  const bool zs = z_in_shared(c, cols);
+  const size_t smem = dec_smem_bytes(c, cols, zs);
+  if (smem > 227 * 1024) return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
+  const size_t need = sqg_decompose_structures_workspace_bytes(c, batch, cols);
+  if (!workspace || ws_bytes < need || ((size_t)workspace & 255))
+    return set_error(SQG_ERR_WORKSPACE, "workspace too small or not 256-byte aligned: need " + std::to_string(need));
+  // every gate list repeats the template's gate types and parameter layout; only the qubits
+  // may differ, and they are checked here so that the kernel indexes in range
+  const int L = c->L, n = c->n;
+  std::vector<Gate> lists((size_t)batch * L);
+  for (long long b = 0; b < batch; b++)
+    for (int g = 0; g < L; g++) {
+      const sqg_gate& in = gates[b * L + g];
+      const Gate& t = c->h_gates[g];
+      const bool ctl = gate_controlled(t.type);
+      if (in.type != t.type || in.param_start != t.pstart)
+        return set_error(SQG_ERR_INVALID_ARGUMENT, "gate list " + std::to_string(b) + " differs from the circuit's gate "
+                                                       "types or parameter layout at gate " + std::to_string(g));
+      if (in.target < 0 || in.target >= n || (ctl && (in.control < 0 || in.control >= n || in.control == in.target)))
+        return set_error(SQG_ERR_INVALID_ARGUMENT, "gate list " + std::to_string(b) + ": qubit out of range at gate " +
+                                                       std::to_string(g));
+      lists[b * L + g] = Gate{in.type, in.target, ctl ? in.control : -1, in.param_start};
+    }
+  const size_t zbytes = zs ? 0 : ((size_t)batch * c->P * c->P * sizeof(double) + 255) / 256 * 256;
+  Gate* dgates = (Gate*)((char*)workspace + zbytes);
+  // pageable source: the call returns once the records are staged, so `lists` may go
+  cudaError_t e = cudaMemcpyAsync(dgates, lists.data(), sizeof(Gate) * lists.size(), cudaMemcpyHostToDevice,
+                                  (cudaStream_t)stream);
+  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("gate lists: ") + cudaGetErrorString(e));
+  DecArgs a = {};
+  a.gates = dgates;
+  a.gstride = L;
+  a.L = L; a.P = c->P; a.n = n; a.N = c->N; a.cols = cols;
+  a.trace_offset = off;
+  a.variant = cost_variant;
+  a.targets = (const double2*)targets;
+  a.tstride = target_stride;
+  a.x = x; a.cost = cost; a.calls = calls; a.iters = iters;
+  a.B = batch;
+  a.tol = tolerance;
+  a.max_calls = max_calls; a.max_outer = max_outer; a.loops = iteration_loops;
+  a.early_stop = stop_at_tolerance;
+  a.seed = seed;
+  a.zglob = zs ? nullptr : (double*)workspace;
+  a.z_in_smem = zs ? 1 : 0;
+  dec_eval_form(c, cols, off, a);
+  return dec_launch<kBfgs>(c, a, batch, smem, stream);
+}
 
 int sqg_decompose_batched_adam(const sqg_circuit* c, const void* targets, int cols, int batch, int trace_offset,
                                int cost_variant, double* x, double* cost, int* evals, int* shifts, double tolerance,

@@ -1,0 +1,121 @@
+"""Structure search (tree_search.py): candidate enumeration and structure construction of
+N_Qubit_Decomposition_Tree_Search (CPU), and on the GPU the many-structure decomposition
+(sqg_decompose_structures) against one-structure batches and a search that recovers a known
+CNOT structure."""
+import importlib
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+@pytest.fixture(scope="module")
+def ts():
+    return importlib.import_module("sequential-quantum-gate-decomposer_gb300.tree_search")
+
+
+@pytest.mark.parametrize("n,topology", [(3, None), (4, None), (4, [(0, 1), (1, 2), (2, 3)]), (5, [(0, 4), (1, 3)])])
+def test_level_codes_equal_the_filtered_enumeration(ts, n, topology):
+    """level_codes = every sequence over the allowed pairs that passes is_unique_structure
+    (at most three equal CNOTs in a row, canonical order of commuting CNOTs), in order."""
+    topo = ts.normalize_topology(topology, n)
+    for level in range(5):
+        brute = [list(c) for c in itertools.product(range(len(topo)), repeat=level)
+                 if ts.is_unique_structure(list(c), topo)]
+        assert ts.level_codes(level, topo).tolist() == brute
+
+
+def test_uniqueness_rules(ts):
+    topo = ts.normalize_topology(None, 4)  # (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
+    assert ts.canonical_prefix_ok([0, 5], topo) == -1   # (0,1) then (2,3): canonical
+    assert ts.canonical_prefix_ok([5, 0], topo) == 0    # commuting pair out of order
+    assert not ts.is_unique_structure([5, 0], topo)
+    assert ts.is_unique_structure([1, 1, 1], topo)
+    assert not ts.is_unique_structure([1, 1, 1, 1], topo)
+    assert ts.normalize_topology([(2, 0)], 3) == [(0, 2)]
+    for bad in ([(0, 0)], [(0, 3)], [(0, 1, 2)]):
+        with pytest.raises(ValueError):
+            ts.normalize_topology(bad, 3)
+
+
+def test_structure_records_match_the_circuit(ts):
+    topo = ts.normalize_topology(None, 4)
+    rng = np.random.default_rng(3)
+    codes = rng.integers(0, len(topo), (5, 4))
+    recs = ts.structure_records(codes, topo, 4)
+    for k in range(5):
+        c = ts.structure_circuit(codes[k], topo, 4)
+        assert np.array_equal(c.gate_records(), recs[k])
+        assert c.get_Parameter_Num() == 6 * 4 + 3 * 4
+        assert len(c.get_Gates()) == 5  # four two-qubit blocks and the final layer
+
+
+@pytest.mark.gpu
+def test_structures_equal_one_structure_batches(sqg, ts):
+    """Instance k of one many-structure launch gives bit for bit what a batch of structure k
+    alone gives for the same instance index, start point, target and seed."""
+    torch = pytest.importorskip("torch")
+    topo = ts.normalize_topology(None, 3)
+    codes = ts.level_codes(3, topo)[[0, 4, 9, 13, 20, 26]]
+    B = codes.shape[0]
+    rng = np.random.default_rng(8)
+    U = O.get_matrix(3, ts.structure_circuit(codes[2], topo, 3).gate_records(), rng.uniform(0, 2 * np.pi, 27))
+    T = np.ascontiguousarray(U.conj().T)
+    x0 = rng.uniform(0, 2 * np.pi, (B, 27))
+    lib = importlib.import_module("sequential-quantum-gate-decomposer_gb300._native")
+    nc = ts.structure_circuit(codes[0], topo, 3).native()
+    recs = np.ascontiguousarray(ts.structure_records(codes, topo, 3))
+    t = torch.from_numpy(T).cuda()
+    x = torch.from_numpy(x0.copy()).cuda()
+    cost = torch.empty(B, dtype=torch.float64, device="cuda")
+    calls = torch.empty(B, dtype=torch.int32, device="cuda")
+    iters = torch.empty(B, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.lib().sqg_decompose_structures_workspace_bytes(nc.handle, B, 8), dtype=torch.uint8,
+                     device="cuda")
+    lib.check(lib.lib().sqg_decompose_structures(nc.handle, recs.ctypes.data, t.data_ptr(), 0, 8, B, 0, 0,
+                                                 x.data_ptr(), cost.data_ptr(), calls.data_ptr(), iters.data_ptr(),
+                                                 1e-8, 10000, 4, 1, 1, 77, ws.data_ptr(), ws.numel(),
+                                                 torch.cuda.current_stream().cuda_stream), "structures")
+    torch.cuda.synchronize()
+    for k in range(B):
+        dec = sqg.BatchedDecomposer(ts.structure_circuit(codes[k], topo, 3), tolerance=1e-8, max_calls=10000,
+                                    max_outer=4, iteration_loops=1, stop_at_tolerance=True)
+        xk, ck, nk = dec.run(np.stack([T] * B), x0, seed=77)
+        torch.cuda.synchronize()
+        assert float(ck[k]) == float(cost[k]) and int(nk[k]) == int(calls[k])
+        assert torch.equal(xk[k], x[k])
+    assert float(cost[2]) < 1e-8  # the structure the target was made from
+    bad = recs.copy()
+    bad[1, 0, 0] = 8  # RY where the circuit has U3
+    with pytest.raises(lib.SQGError, match="differs"):
+        lib.check(lib.lib().sqg_decompose_structures(nc.handle, bad.ctypes.data, t.data_ptr(), 0, 8, B, 0, 0,
+                                                     x.data_ptr(), cost.data_ptr(), calls.data_ptr(), None, 1e-8,
+                                                     10, 1, 1, 1, 0, ws.data_ptr(), ws.numel(),
+                                                     torch.cuda.current_stream().cuda_stream), "structures")
+    bad = recs.copy()
+    bad[0, 2, 2] = bad[0, 2, 1]  # CNOT with control == target
+    with pytest.raises(lib.SQGError, match="out of range"):
+        lib.check(lib.lib().sqg_decompose_structures(nc.handle, bad.ctypes.data, t.data_ptr(), 0, 8, B, 0, 0,
+                                                     x.data_ptr(), cost.data_ptr(), calls.data_ptr(), None, 1e-8,
+                                                     10, 1, 1, 1, 0, ws.data_ptr(), ws.numel(),
+                                                     torch.cuda.current_stream().cuda_stream), "structures")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,seq", [(3, [(0, 1), (1, 2)]), (4, [(0, 1), (2, 3), (1, 2)]), (2, [(0, 1)])])
+def test_tree_search_recovers_a_known_structure(sqg, ts, n, seq):
+    topo = ts.normalize_topology(None, n)
+    code = [topo.index(p) for p in seq]
+    c = ts.structure_circuit(code, topo, n)
+    rng = np.random.default_rng(len(seq) + n)
+    U = O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
+    dec = sqg.N_Qubit_Decomposition_Tree_Search(np.ascontiguousarray(U.conj().T),
+                                                config={"optimization_tolerance": 1e-8, "random_seed": 1})
+    dec.Start_Decomposition()
+    assert dec.get_Decomposition_Error() < 1e-8
+    assert len(dec.best_cnot_sequence) <= len(seq)
+    assert dec.levels_done == len(dec.best_cnot_sequence) + 1
+    x = dec.get_Optimized_Parameters()
+    assert abs(O.cost(n, dec.get_Circuit().gate_records(), x, dec.get_Unitary())) < 1e-8
