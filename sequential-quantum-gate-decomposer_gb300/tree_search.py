@@ -255,3 +255,125 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
         self.decomposition_error = self.Optimization_Problem(best_x)
         self.best_cnot_sequence = [self.topology[int(d)] for d in best_code]
         return 0
+
+
+def insert_into_best_solution(best_solutions, code, minimum):
+    """Keeps (code, minimum) pairs sorted by minimum, at most 40
+    (N_Qubit_Decomposition_Tabu_Search::insert_into_best_solution): the pair goes before the
+    first entry with a larger minimum (into an empty list at the front; after the last entry
+    it is not added)."""
+    if not best_solutions:
+        best_solutions.insert(0, (tuple(code), minimum))
+    for i, (_, m) in enumerate(best_solutions):
+        if m > minimum:
+            best_solutions.insert(i, (tuple(code), minimum))
+            break
+    if len(best_solutions) > 40:
+        best_solutions.pop()
+
+
+def determine_mutated_structures(code, n_pairs, level_limit, tested):
+    """Untested neighbours of a CNOT sequence: every single-position change, every single
+    removal and, below the level limit, every one-CNOT extension at the end
+    (determine_mutated_structures)."""
+    code = tuple(int(v) for v in code)
+    out = []
+    for i in range(len(code)):
+        for e in range(n_pairs):
+            m = code[:i] + (e,) + code[i + 1:]
+            if m not in tested:
+                out.append(m)
+    for i in range(len(code)):
+        m = code[:i] + code[i + 1:]
+        if m not in tested:
+            out.append(m)
+    if len(code) == level_limit:
+        return out
+    for e in range(n_pairs):
+        m = code + (e,)
+        if m not in tested:
+            out.append(m)
+    return out
+
+
+def draw_gate_structure_from_list(codes, rng):
+    """Removes and returns one sequence, drawn with weight 4 * (len(codes[0]) - len(code))
+    (draw_gate_structure_from_list): a uniform integer r in [0, sum of weights] picks the first
+    entry whose running weight sum exceeds r, else the first entry (also when the weights sum
+    to a negative number, where the reference's unsigned draw exceeds every partial sum)."""
+    if not codes:
+        raise ValueError("the list of gate structures is empty")
+    levels = len(codes[0])
+    weights = [4 * levels - 4 * len(c) for c in codes]
+    total = sum(weights)
+    chosen = 0
+    if total >= 0:
+        r = int(rng.integers(0, total + 1))
+        part = 0
+        for i, w in enumerate(weights):
+            part += w
+            if r < part:
+                chosen = i
+                break
+    return codes.pop(chosen)
+
+
+class N_Qubit_Decomposition_Tabu_Search(N_Qubit_Decomposition_Tree_Search):
+    """Drop-in for squander.N_Qubit_Decomposition_Tabu_Search(Umtx, qbit_num=-1, topology=None,
+    config=None, accelerator_num=0): the tabu walk over CNOT structures of
+    N_Qubit_Decomposition_Tabu_Search::tabu_search_over_gate_structures
+    (src-cpp/decomposition/N_Qubit_Decomposition_Tabu_Search.cpp:160-400, use_osr = 0).  Each step
+    decomposes one structure on the device (one k_decompose launch: BFGS up to five qubits,
+    the graph-driven ADAM loop above), accepts it when its minimum is lower, or else with
+    probability exp(-(f - f_current)), keeps the 40 best structures, and draws the next
+    structure among the untested neighbours of the current one.  Random draws come from the
+    decomposer's seeded generator instead of the reference's default_random_engine and
+    random_device."""
+
+    def Start_Decomposition(self):
+        tol = float(self.config.get("optimization_tolerance", self.optimization_tolerance))
+        target = self.evaluator().target
+        max_inner = int(self.config.get("max_inner_iterations_bfgs", self.config.get("max_inner_iterations", 10000)))
+        max_outer = int(self.config.get("max_outer_iterations", 4 if self.qbit_num <= 5 else 1))
+        loops = int(self.config.get("max_iteration_loops", 3 if self.qbit_num == 2 else 1))
+        T = len(self.topology)
+        code = ()
+        best_code, best_x = (), None
+        current = math.inf
+        possible, tested, best_solutions = [], set(), []
+        accepted = {}  # parameters of every accepted structure
+        self.structures_tested = 0
+        while True:
+            codes = np.asarray([code], dtype=np.int64).reshape(1, len(code))
+            if self.qbit_num <= 5:
+                f, _, x, ev = self._decompose_level_small(codes, tol, max_inner, max_outer, loops, target)
+            else:
+                f, _, x, ev = self._decompose_level_large(codes, tol, target)
+            self.num_iters += ev
+            self.structures_tested += 1
+            tested.add(code)
+            if f < current or self.rng.uniform() < math.exp(-1.0 * (f - current)):
+                current, best_code, best_x = f, code, x
+                accepted[code] = x
+                possible = []
+                insert_into_best_solution(best_solutions, code, f)
+            if current < tol:
+                break
+            if not possible:
+                possible = determine_mutated_structures(best_code, T, self.level_limit, tested)
+            if not possible:
+                while best_solutions:
+                    best_code, current = best_solutions.pop(0)
+                    possible = determine_mutated_structures(best_code, T, self.level_limit, tested)
+                    if possible or not best_solutions:
+                        break
+            if not possible:
+                break
+            code = draw_gate_structure_from_list(possible, self.rng)
+        best_x = accepted[best_code]  # the structure may come back from the list of best ones
+        self.circuit = structure_circuit(best_code, self.topology, self.qbit_num)
+        self._evaluator = None
+        self.optimized_parameters = best_x
+        self.decomposition_error = self.Optimization_Problem(best_x)
+        self.best_cnot_sequence = [self.topology[int(d)] for d in best_code]
+        return 0

@@ -119,3 +119,48 @@ def test_tree_search_recovers_a_known_structure(sqg, ts, n, seq):
     assert dec.levels_done == len(dec.best_cnot_sequence) + 1
     x = dec.get_Optimized_Parameters()
     assert abs(O.cost(n, dec.get_Circuit().gate_records(), x, dec.get_Unitary())) < 1e-8
+
+
+def test_tabu_helpers(ts):
+    best = []
+    ts.insert_into_best_solution(best, (1,), 0.5)
+    ts.insert_into_best_solution(best, (2,), 0.2)
+    ts.insert_into_best_solution(best, (3,), 0.9)  # larger than every entry: not added
+    assert best == [((2,), 0.2), ((1,), 0.5)]
+    for k in range(50):
+        ts.insert_into_best_solution(best, (k, k), 0.1 - k * 1e-3)
+    assert len(best) == 40 and best[0][1] == min(m for _, m in best)
+    tested = {(0, 1)}
+    mut = ts.determine_mutated_structures((0, 1), 3, 14, tested)
+    assert (0, 1) not in mut and (2, 1) in mut and (1,) in mut and (0, 1, 2) in mut
+    assert len(mut) == 4 + 2 + 3  # changes, removals, extensions
+    assert all(len(c) <= 2 for c in ts.determine_mutated_structures((0, 1), 3, 2, tested))
+    rng = np.random.default_rng(0)
+    codes = [(0,), (1,), (2,)]  # equal lengths: all weights 0, the first is drawn
+    assert ts.draw_gate_structure_from_list(codes, rng) == (0,) and len(codes) == 2
+    codes = [(0, 1), (1,), (0, 1, 2)]  # weights 0, 4, -4: r = 0 < 4 picks the removal
+    assert ts.draw_gate_structure_from_list(codes, rng) == (1,)
+    codes = [(0,), (0, 1), (0, 2)]  # weights 0, -4, -4: negative sum, the first is drawn
+    assert ts.draw_gate_structure_from_list(codes, rng) == (0,)
+    draws = set()
+    for seed in range(20):
+        codes = [(0, 1), (1,), (0,), (2, 2)]  # weights 0, 4, 4, 0
+        draws.add(ts.draw_gate_structure_from_list(codes, np.random.default_rng(seed)))
+    assert draws <= {(1,), (0,), (0, 1)} and (1,) in draws and (0,) in draws
+
+
+@pytest.mark.gpu
+def test_tabu_search_reaches_tolerance(sqg, ts):
+    n, seq = 3, [(0, 1), (1, 2)]
+    topo = ts.normalize_topology(None, n)
+    c = ts.structure_circuit([topo.index(p) for p in seq], topo, n)
+    rng = np.random.default_rng(12)
+    U = O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
+    dec = sqg.N_Qubit_Decomposition_Tabu_Search(np.ascontiguousarray(U.conj().T),
+                                                config={"optimization_tolerance": 1e-8, "random_seed": 4,
+                                                        "tree_level_max": 4})
+    dec.Start_Decomposition()
+    assert dec.get_Decomposition_Error() < 1e-8
+    assert dec.structures_tested >= 2
+    x = dec.get_Optimized_Parameters()
+    assert abs(O.cost(n, dec.get_Circuit().gate_records(), x, dec.get_Unitary())) < 1e-8
