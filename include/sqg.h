@@ -218,6 +218,24 @@ int sqg_decompose_batched(const sqg_circuit* circuit, const void* targets_dev, i
                           int max_calls, int max_outer, int iteration_loops, int stop_at_tolerance,
                           unsigned long long seed, void* workspace_dev, size_t workspace_bytes, void* stream);
 
+/* One BFGS decomposition for any qbit_num the gradient supports (<= 12), run on the device as
+ * a single CUDA graph launch: a conditional while-node whose body evaluates the cost and
+ * gradient (the kernels of sqg_cost_grad) and then advances BFGS_Powell (Powell's Z update, the
+ * reference line search, the restarts) on one CTA up to the next point to evaluate.  Replaces
+ * the host loop of solve_layer_optimization_problem_BFGS (src-cpp/optimization_engines/
+ * BFGS.cpp:42-152, src-cpp/common/BFGS_Powell.cpp:70-396).  Semantics and parameters as
+ * sqg_decompose_batched with batch 1 (same random stream for the restart perturbations); up to
+ * five qubits and for targets with cols >= 3N/4 the result is bit-identical to
+ * sqg_decompose_batched.  The workspace (256-byte aligned, sqg_bfgs_loop_workspace_bytes) holds
+ * the state, the P x P matrix Z and the evaluation scratch and must stay untouched until the
+ * stream reaches the end of the call.  Asynchronous on stream. */
+size_t sqg_bfgs_loop_workspace_bytes(const sqg_circuit* circuit, int cols);
+int sqg_decompose_bfgs_loop(const sqg_circuit* circuit, const void* target_dev, int cols, int trace_offset,
+                            int cost_variant, double* x_dev, double* cost_dev, int* calls_dev, int* iters_dev,
+                            double tolerance, int max_calls, int max_outer, int iteration_loops,
+                            int stop_at_tolerance, unsigned long long seed, void* workspace_dev,
+                            size_t workspace_bytes, void* stream);
+
 /* Batched BFGS decompositions of many gate STRUCTURES at once (the inner loop of the
  * structure-search decomposers, N_Qubit_Decomposition_Tree_Search::
  * tree_search_over_gate_structures, src-cpp/decomposition/N_Qubit_Decomposition_Tree_Search.cpp:

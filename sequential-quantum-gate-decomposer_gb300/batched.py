@@ -112,6 +112,38 @@ def adam_decompose_graph(circuit, target_udag, x0, tolerance=1e-8, max_iters=100
     return x, cost, evals, shifts
 
 
+def bfgs_decompose_graph(circuit, target_udag, x0, tolerance=1e-8, max_calls=10000, max_outer=4, iteration_loops=1,
+                         stop_at_tolerance=True, seed=0, trace_offset=0, cost_variant=0, workspace=None, stream=None):
+    """One BFGS decomposition (the driver of BatchedDecomposer for a single target) for any
+    register the gradient supports, run on the device as a single CUDA graph launch
+    (sqg_decompose_bfgs_loop: a conditional while-node over [cost + gradient kernels, BFGS
+    step]).  Returns CUDA tensors (x (P,) best point, cost (1,), calls (1,) int32, BFGS
+    iterations (1,) int32); asynchronous on stream."""
+    dev.require_cuda()
+    native = circuit.native() if isinstance(circuit, Circuit) else circuit
+    t = dev.to_device_complex(target_udag)
+    if t.dim() != 2 or t.shape[0] != (1 << native.qbit_num):
+        raise ValueError("target must be (2**qbit_num, cols)")
+    x = dev.to_device_real(x0).reshape(-1).clone()
+    if x.numel() != native.param_num:
+        raise ValueError("x0 must hold %d parameters" % native.param_num)
+    cost = dev.torch.empty(1, dtype=dev.torch.float64, device="cuda")
+    calls = dev.torch.empty(1, dtype=dev.torch.int32, device="cuda")
+    iters = dev.torch.empty(1, dtype=dev.torch.int32, device="cuda")
+    lib = _native.lib()
+    cols = int(t.shape[1])
+    ws = (workspace or dev.Workspace()).get(lib.sqg_bfgs_loop_workspace_bytes(native.handle, cols))
+    _native.check(lib.sqg_decompose_bfgs_loop(
+        native.handle, dev.ptr(t), cols, int(trace_offset), int(cost_variant), dev.ptr(x), dev.ptr(cost),
+        dev.ptr(calls), dev.ptr(iters), float(tolerance), int(max_calls), int(max_outer), int(iteration_loops),
+        1 if stop_at_tolerance else 0, int(seed) & 0xFFFFFFFFFFFFFFFF, dev.ptr(ws), ws.numel(),
+        dev.stream_ptr(stream)), "sqg_decompose_bfgs_loop")
+    if stream is not None:
+        ws.record_stream(stream)
+        t.record_stream(stream)
+    return x, cost, calls, iters
+
+
 def random_start(B, P, rng):
     """RANDOM initial guess of Decomposition_Base (U[0, 2 pi), Decomposition_Base.cpp:415-436)."""
     return rng.uniform(0.0, 2 * np.pi, (B, P))

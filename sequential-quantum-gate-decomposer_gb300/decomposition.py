@@ -17,7 +17,7 @@ from . import _device as dev
 from . import _native
 from .circuit import Circuit, combined_unitary_device
 from .evaluator import FROBENIUS_NORM, SUPPORTED_VARIANTS, CostEvaluator
-from .batched import BatchedDecomposer, adam_decompose_graph
+from .batched import BatchedDecomposer, adam_decompose_graph, bfgs_decompose_graph
 from .optim import adam_squander, bfgs_powell
 
 _GUESS = {"zeros": "ZEROS", "random": "RANDOM", "close_to_zero": "CLOSE_TO_ZERO"}
@@ -341,8 +341,8 @@ class N_Qubit_Decomposition_custom:
 
         Every outer iteration runs on the device without a host round trip per evaluation:
         ADAM as one CUDA graph launch (batched.adam_decompose_graph), BFGS up to five qubits
-        as one k_decompose launch of iteration_loops runs.  BFGS above five qubits drives
-        the device cost and gradient from the host (optim.bfgs_powell).  The outer loop and
+        as one k_decompose launch of iteration_loops runs and above five qubits as one CUDA
+        graph launch of those runs (batched.bfgs_decompose_graph).  The outer loop and
         its tolerance test stay on the host, so each launch is bounded by one outer
         iteration's evaluation budget."""
         P = self.get_Parameter_Num()
@@ -392,7 +392,17 @@ class N_Qubit_Decomposition_custom:
                         self.num_iters += calls
                         if f < best_f:
                             best_f, best_x = f, x
-                if self.qbit_num > 5 or self._host_loops:
+                if self.qbit_num > 5 and not self._host_loops:
+                    # the BFGS runs of one outer iteration as one CUDA graph launch
+                    xd, cd, ed, _it = bfgs_decompose_graph(
+                        self.circuit, target, guess, tol, max_inner, max_outer=1, iteration_loops=loops,
+                        stop_at_tolerance=False, seed=int(self.rng.integers(1 << 62)),
+                        trace_offset=self.trace_offset, cost_variant=self.cost_variant, workspace=self._loop_ws)
+                    f, calls = float(cd.item()), int(ed.item())
+                    self.num_iters += calls
+                    if f < best_f:
+                        best_f, best_x = f, xd.cpu().numpy()
+                elif self.qbit_num > 5 or self._host_loops:
                     for _loop in range(loops):
                         f, calls = bfgs_powell(self._fg, guess, max_inner)
                         self.num_iters += calls

@@ -1,6 +1,7 @@
-"""Graph-driven single-target ADAM decomposition (sqg_decompose_adam_loop: one CUDA graph
-launch per decomposition) against the oracle's restatement of SQUANDER's ADAM engine, and
-the drop-in Start_Decomposition on its device loops against its host-driven loops."""
+"""Graph-driven single-target decompositions (one CUDA graph launch per decomposition): the ADAM
+engine (sqg_decompose_adam_loop) against the oracle's restatement of it, BFGS
+(sqg_decompose_bfgs_loop) against k_decompose and the host-driven BFGS, and the drop-in
+Start_Decomposition on its device loops against its host-driven loops."""
 import importlib
 
 import numpy as np
@@ -148,3 +149,66 @@ def test_dropin_device_loops_match_host_loops(sqg, wl, n, optimizer):
         assert np.allclose(xd, xh, atol=1e-7)
     else:
         assert fd < 1e-8 and fh < 1e-8
+
+
+@pytest.mark.parametrize("n,blocks,max_outer,loops,early", [(3, 4, 4, 1, True), (3, 6, 2, 3, False), (4, 3, 2, 2, True)])
+def test_graph_bfgs_equals_k_decompose(sqg, wl, batched, n, blocks, max_outer, loops, early):
+    """Up to five qubits the graph loop evaluates with the same kernel and reduction order as
+    k_decompose: every run, restart and perturbation gives the same bits."""
+    rng = np.random.default_rng(300 + 10 * n + blocks)
+    c = wl.cnot_u3_ansatz(n, blocks)
+    P = c.get_Parameter_Num()
+    T = np.ascontiguousarray(wl.haar_unitary(1 << n, rng).conj().T)  # not reachable: all runs happen
+    x0 = rng.uniform(0, 2 * np.pi, P)
+    dec = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=200, max_outer=max_outer, iteration_loops=loops,
+                                stop_at_tolerance=early)
+    xk, ck, nk = dec.run(T[None], x0[None], seed=21)
+    xg, cg, ng, ig = batched.bfgs_decompose_graph(c, T, x0, tolerance=1e-8, max_calls=200, max_outer=max_outer,
+                                                  iteration_loops=loops, stop_at_tolerance=early, seed=21)
+    torch.cuda.synchronize()
+    assert int(ng.item()) == int(nk[0].item()) and int(ig.item()) == int(dec.iters[0].item())
+    assert float(cg.item()) == float(ck[0].item())
+    assert torch.equal(xg, xk[0])
+    assert int(ng.item()) >= max_outer * loops
+
+
+@pytest.mark.parametrize("n,blocks", [(6, 4), (6, 25)])
+def test_graph_bfgs_above_five_qubits_follows_host_bfgs(sqg, wl, batched, n, blocks):
+    """Tile-kernel evaluation in the graph body (P = 42 on 64 threads, P = 168 on 256): one BFGS
+    run follows the host-driven BFGS_Powell restatement over the same cost and gradient."""
+    optim = importlib.import_module("sequential-quantum-gate-decomposer_gb300.optim")
+    rng = np.random.default_rng(600 + blocks)
+    c = wl.cnot_u3_ansatz(n, blocks)
+    P = c.get_Parameter_Num()
+    T = np.ascontiguousarray(O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, P)).conj().T)
+    x0 = rng.uniform(0, 2 * np.pi, P)
+    ev = sqg.CostEvaluator(c, T)
+
+    def fg(x):
+        cost, grad = ev.cost_grad(torch.from_numpy(x).cuda())
+        return float(cost.item()), grad.reshape(-1).cpu().numpy()
+
+    xh = x0.copy()
+    fh, nh = optim.bfgs_powell(fg, xh, 40)
+    xg, cg, ng, _ = batched.bfgs_decompose_graph(c, T, x0, max_calls=40, max_outer=1, iteration_loops=1,
+                                                 stop_at_tolerance=False, seed=1)
+    torch.cuda.synchronize()
+    assert int(ng.item()) == nh
+    assert np.isclose(float(cg.item()), fh, rtol=1e-7, atol=1e-12)
+    assert np.allclose(xg.cpu().numpy(), xh, atol=1e-6)
+
+
+def test_dropin_bfgs_above_five_qubits_on_the_device(sqg, wl):
+    rng = np.random.default_rng(66)
+    n, c = 6, wl.cnot_u3_ansatz(6, 3)
+    P = c.get_Parameter_Num()
+    xt = rng.uniform(0, 2 * np.pi, P)
+    T = np.ascontiguousarray(O.get_matrix(n, c.gate_records(), xt).conj().T)
+    dec = sqg.N_Qubit_Decomposition_custom(T, config={"optimization_tolerance": 1e-8, "random_seed": 3})
+    dec.set_Gate_Structure(c)
+    dec.set_Optimizer("BFGS")
+    dec.max_outer_iterations = 4
+    dec.set_Optimized_Parameters(xt + 0.05 * rng.standard_normal(P))
+    dec.Start_Decomposition()
+    assert dec.get_Decomposition_Error() < 1e-8
+    assert abs(O.cost(n, c.gate_records(), dec.get_Optimized_Parameters(), T)) < 1e-8
