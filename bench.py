@@ -318,6 +318,7 @@ def bench_ours(args):
         line["cost_grad_uneven"] = bench_ragged(sqg, wl, torch)
         line["cost_grad_n10"] = bench_cost_grad_n10(sqg, wl, torch)
         line["decompose_n4_single"] = bench_single_n4(sqg, wl, torch)
+        line["dropin_loops"] = bench_dropin_loops(sqg, wl, torch)
         line["state_vector_n24"] = bench_state_vector(sqg, wl, torch)
         line["decompose_16384_one_launch"] = bench_large_batch(sqg, wl, torch, ansatz, targets)
     if not args.skip_cpu:
@@ -469,9 +470,9 @@ def bench_ragged(sqg, wl, torch):
 
 
 def bench_single_n4(sqg, wl, torch):
-    """BASELINE config 1: one 4-qubit Haar target, U3 layer + 40 nearest-neighbour CNOT
-    blocks (P = 252), BFGS towards cost < 1e-8 through the drop-in class (host BFGS, one
-    GPU cost+gradient call per evaluation) and through the device decomposer (B = 1)."""
+    """One 4-qubit Haar target, U3 layer + 40 nearest-neighbour CNOT blocks (P = 252), BFGS
+    towards cost < 1e-8 through the drop-in class with its host-driven loop (one GPU
+    cost+gradient call per evaluation) and through the device decomposer (B = 1)."""
     rng = np.random.default_rng(11)
     U = wl.haar_unitary(16, rng)
     c = wl.cnot_u3_ansatz(4, 40)
@@ -480,6 +481,7 @@ def bench_single_n4(sqg, wl, torch):
     d = sqg.N_Qubit_Decomposition_custom(U.conj().T, config={"optimization_tolerance": 1e-8, "max_outer_iterations": 1,
                                                              "max_inner_iterations": 2000})
     d.set_Gate_Structure(c)
+    d._host_loops = True  # BFGS driven from the host, one GPU cost+gradient call per evaluation
     d.set_Optimized_Parameters(x0)
     t0 = time.perf_counter()
     d.Start_Decomposition()
@@ -500,6 +502,59 @@ def bench_single_n4(sqg, wl, torch):
                             "final_cost": float(cost.item())},
             "note": "40 CNOTs are below the 61-CNOT lower bound for generic 4-qubit unitaries, so the cost "
                     "cannot reach 1e-8 on a Haar target"}
+
+
+def bench_dropin_loops(sqg, wl, torch):
+    """Single decompositions through the drop-in class above five qubits: the device loops (one
+    CUDA graph launch per outer iteration) against the host-driven loops over the same GPU
+    cost and gradient, per evaluation; and the structure search of the tree-search class on a
+    3-qubit target made from a 5-CNOT structure (all candidates of a level in one launch)."""
+    out = {}
+    for n, blocks, opt, iters in [(6, 20, "BFGS", 1000), (6, 20, "ADAM", 1000), (8, 120, "BFGS", 60)]:
+        rng = np.random.default_rng(n + blocks)
+        c = wl.cnot_u3_ansatz(n, blocks)
+        P = c.get_Parameter_Num()
+        T = np.ascontiguousarray(wl.haar_unitary(1 << n, rng).conj().T)
+        start = rng.uniform(0, 2 * np.pi, P)
+        row = {"qbit_num": n, "params": P}
+        for host in (False, True):
+            d = sqg.N_Qubit_Decomposition_custom(T, config={"random_seed": 1, "max_inner_iterations": iters})
+            d.set_Gate_Structure(c)
+            d.set_Optimizer(opt)
+            d.max_outer_iterations = 1
+            d._host_loops = host
+            d.set_Optimized_Parameters(start)
+            d.Start_Decomposition()  # warm-up: graph, kernels
+            d.num_iters = 0
+            d.set_Optimized_Parameters(start)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d.Start_Decomposition()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            ev = d.get_Num_of_Iters()
+            row["host_loop" if host else "device_loop"] = {"evals": ev, "seconds": dt, "us_per_eval": 1e6 * dt / ev}
+        row["speedup"] = row["host_loop"]["us_per_eval"] / row["device_loop"]["us_per_eval"]
+        out["%s_n%d_P%d" % (opt.lower(), n, P)] = row
+    ts = importlib.import_module(PKG + ".tree_search")
+    topo = ts.normalize_topology(None, 3)
+    rng = np.random.default_rng(5)
+    code = [0, 2, 1, 0, 2]
+    c = ts.structure_circuit(code, topo, 3)
+    U = c.get_Matrix(rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
+    d = sqg.N_Qubit_Decomposition_Tree_Search(np.ascontiguousarray(U.conj().T),
+                                              config={"optimization_tolerance": 1e-8, "random_seed": 2})
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d.Start_Decomposition()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    cand = sum(ts.level_codes(lv, topo).shape[0] for lv in range(d.levels_done))
+    out["tree_search_3q"] = {"config": "3-qubit target from a 5-CNOT structure, level search over all pairs",
+                             "seconds": dt, "levels": d.levels_done, "structures": cand,
+                             "structures_per_s": cand / dt, "cnots_found": len(d.best_cnot_sequence),
+                             "error": d.get_Decomposition_Error()}
+    return out
 
 
 def bench_cost_grad_n10(sqg, wl, torch):
@@ -683,6 +738,13 @@ def profile_case(case, profile_calls=60):
         t = e0.elapsed_time(e1) / 20 / 1e3
         print(json.dumps({"mlp_gemm_tc": {"M": 4096, "N": 1024, "K": 1024, "seconds": t,
                                           "tflops": 2.0 * 4096 * 1024 * 1024 / t / 1e12}}))
+    elif case == "dropin_bfgs_n6":
+        batched = importlib.import_module(PKG + ".batched")
+        c = wl.cnot_u3_ansatz(6, 20)
+        P = c.get_Parameter_Num()
+        T = np.ascontiguousarray(wl.haar_unitary(64, rng).conj().T)
+        batched.bfgs_decompose_graph(c, T, rng.uniform(0, 2 * np.pi, P), max_calls=profile_calls, max_outer=1,
+                                     stop_at_tolerance=False)
     elif case == "cost_grad":
         c = wl.cnot_u3_ansatz(8, 60)
         P = c.get_Parameter_Num()
@@ -696,7 +758,8 @@ def profile_case(case, profile_calls=60):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe-fp64", action="store_true", help="print the live FP64 FMA peak by active lanes")
-    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad", "mlp_gemm"], default=None)
+    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad", "mlp_gemm", "dropin_bfgs_n6"],
+                    default=None)
     ap.add_argument("--profile-calls", type=int, default=60,
                     help="evaluations per BFGS run in the decompose profile case (below 60: no tolerance stop)")
     ap.add_argument("--gpus", type=int, default=1)

@@ -11,7 +11,9 @@ outer iterations up to five qubits), stopping at the first level that reaches th
 (:622-776 with use_osr = use_graph_search = 0, tree_search_over_gate_structures :1269-1451).
 
 Here every candidate structure of a level is decomposed on the GPU in one launch
-(sqg_decompose_structures: one CTA per structure, each with its own gate list), in chunks.
+(sqg_decompose_structures: one CTA per structure, each with its own gate list), in chunks;
+consecutive small levels (together at most one wave of resident CTAs) run at the same time on
+separate streams, and the lowest level that reaches the tolerance still decides.
 Among the structures that reach the tolerance the one with the lowest cost is kept.  The
 reference's threads instead stop at whichever solution they find first, so ties may resolve
 differently.  The reference's default operator-Schmidt-rank bounds and best-first graph search
@@ -172,38 +174,62 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
         self.level_limit = min(max(int(self.config.get("tree_level_max", 14)), 0), 14)
         self.levels_done = 0
 
+    def _launch_structures(self, codes, tol, max_inner, max_outer, loops, target, stream=None):
+        """One launch of BFGS decompositions of the structures of `codes` (one level, at most
+        `chunk` of them) on `stream`.  Returns the device results (x, cost, calls) and the
+        buffers that must outlive the launch."""
+        n, topo = self.qbit_num, self.topology
+        circ = structure_circuit(codes[0], topo, n)
+        nc = circ.native()
+        P, B = nc.param_num, codes.shape[0]
+        lib = _native.lib()
+        recs = np.ascontiguousarray(structure_records(codes, topo, n))
+        x = dev.to_device_real(self.rng.uniform(0.0, 2 * math.pi, (B, P)))
+        cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
+        calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
+        w = dev.Workspace().get(lib.sqg_decompose_structures_workspace_bytes(nc.handle, B, target.shape[1]))
+        _native.check(lib.sqg_decompose_structures(
+            nc.handle, recs.ctypes.data, dev.ptr(target), 0, target.shape[1], B, self.trace_offset,
+            self.cost_variant, dev.ptr(x), dev.ptr(cost), dev.ptr(calls), None, tol, max_inner, max_outer, loops, 0,
+            int(self.rng.integers(1 << 62)), dev.ptr(w), w.numel(), dev.stream_ptr(stream)),
+            "sqg_decompose_structures")
+        return (x, cost, calls), (circ, w)
+
+    @staticmethod
+    def _collect(results, offset=0):
+        """(best cost, its index + offset, best point, evaluations) of one launch's results."""
+        x, cost, calls = results
+        c = cost.cpu().numpy()
+        k = int(np.argmin(c))
+        return float(c[k]), offset + k, x[k].cpu().numpy(), int(calls.sum().item())
+
     def _decompose_level_small(self, codes, tol, max_inner, max_outer, loops, target):
         """BFGS decompositions of every structure of `codes` in chunks of one launch each
         (qbit_num <= 5).  Returns (best cost, its code index, best point, evaluations)."""
-        n, topo = self.qbit_num, self.topology
-        nc = structure_circuit(codes[0], topo, n).native()
-        P = nc.param_num
-        lib = _native.lib()
-        ws = dev.Workspace()
         best = (math.inf, -1, None)
         evals = 0
         for s in range(0, codes.shape[0], self.chunk):
-            part = codes[s:s + self.chunk]
-            B = part.shape[0]
-            recs = np.ascontiguousarray(structure_records(part, topo, n))
-            x = dev.to_device_real(self.rng.uniform(0.0, 2 * math.pi, (B, P)))
-            cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
-            calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
-            iters = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
-            w = ws.get(lib.sqg_decompose_structures_workspace_bytes(nc.handle, B, target.shape[1]))
-            _native.check(lib.sqg_decompose_structures(
-                nc.handle, recs.ctypes.data, dev.ptr(target), 0, target.shape[1], B, self.trace_offset,
-                self.cost_variant, dev.ptr(x), dev.ptr(cost), dev.ptr(calls), dev.ptr(iters), tol, max_inner,
-                max_outer, loops, 0, int(self.rng.integers(1 << 62)), dev.ptr(w), w.numel(), dev.stream_ptr()),
-                "sqg_decompose_structures")
-            c = cost.cpu().numpy()
-            evals += int(calls.sum().item())
-            k = int(np.argmin(c))
-            if c[k] < best[0]:
-                best = (float(c[k]), s + k, x[k].cpu().numpy())
+            res, _keep = self._launch_structures(codes[s:s + self.chunk], tol, max_inner, max_outer, loops, target)
+            f, k, x, ev = self._collect(res, s)
+            evals += ev
+            if f < best[0]:
+                best = (f, k, x)
             if best[0] < tol:
                 break
         return best[0], best[1], best[2], evals
+
+    def _decompose_levels_concurrently(self, level_list, tol, max_inner, max_outer, loops, target):
+        """Small levels (together at most one wave of resident CTAs) launched at once, one stream
+        per level: a level's launch lasts as long as its slowest decomposition, so running
+        them side by side costs no more than the slowest one.  Returns the per-level
+        (best cost, index, best point, evaluations) in level order."""
+        streams = [dev.torch.cuda.Stream() for _ in level_list]
+        launched = []
+        for (lv, codes), st in zip(level_list, streams):
+            launched.append(self._launch_structures(codes, tol, max_inner, max_outer, loops, target, stream=st))
+        for st in streams:
+            st.synchronize()
+        return [self._collect(res) for res, _keep in launched]
 
     def _decompose_level_large(self, codes, tol, target):
         """ADAM decompositions (the reference's choice above five qubits: max_inner_iterations
@@ -235,20 +261,39 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
         max_outer = int(self.config.get("max_outer_iterations", 4 if self.qbit_num <= 5 else 1))
         loops = int(self.config.get("max_iteration_loops", 3 if self.qbit_num == 2 else 1))
         best_f, best_code, best_x = math.inf, None, None
-        for level in range(self.level_limit + 1):
+        props = dev.torch.cuda.get_device_properties(dev.torch.cuda.current_device())
+        wave = 8 * props.multi_processor_count  # resident decomposition CTAs (8 per SM)
+        level = 0
+        while level <= self.level_limit:
             codes = level_codes(level, self.topology)
-            if codes.shape[0] == 0:
+            if codes.shape[0] == 0:  # e.g. one qubit pair: four equal CNOTs in a row are excluded
+                level += 1
                 continue
-            if self.qbit_num <= 5:
-                f, k, x, ev = self._decompose_level_small(codes, tol, max_inner, max_outer, loops, target)
+            group = [(level, codes)]
+            total = codes.shape[0]
+            while self.qbit_num <= 5 and group[-1][0] < self.level_limit:
+                nxt = level_codes(group[-1][0] + 1, self.topology)
+                if nxt.shape[0] == 0 or total + nxt.shape[0] > wave:
+                    break
+                group.append((group[-1][0] + 1, nxt))
+                total += nxt.shape[0]
+            if len(group) > 1:
+                results = self._decompose_levels_concurrently(group, tol, max_inner, max_outer, loops, target)
+            elif self.qbit_num <= 5:
+                results = [self._decompose_level_small(codes, tol, max_inner, max_outer, loops, target)]
             else:
-                f, k, x, ev = self._decompose_level_large(codes, tol, target)
-            self.num_iters += ev
-            self.levels_done = level + 1
-            if f < best_f:
-                best_f, best_code, best_x = f, codes[k], x
+                results = [self._decompose_level_large(codes, tol, target)]
+            for (lv, lcodes), (f, k, x, ev) in zip(group, results):
+                # levels above the solving one ran ahead on idle SMs: not counted as the search's work
+                self.num_iters += ev
+                self.levels_done = lv + 1
+                if f < best_f:
+                    best_f, best_code, best_x = f, lcodes[k], x
+                if best_f < tol:
+                    break
             if best_f < tol:
                 break
+            level = group[-1][0] + 1
         self.circuit = structure_circuit(best_code, self.topology, self.qbit_num)
         self._evaluator = None
         self.optimized_parameters = best_x
