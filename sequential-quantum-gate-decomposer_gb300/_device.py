@@ -27,6 +27,15 @@ def stream_ptr(stream=None):
     return int(s.cuda_stream)
 
 
+def after_current(stream):
+    """Makes `stream` (if given and not the current stream) wait for the work queued so far on
+    the current stream, where the inputs of a launch were copied or produced."""
+    if stream is not None:
+        cur = torch.cuda.current_stream()
+        if stream != cur:
+            stream.wait_stream(cur)
+
+
 def ptr(t):
     return int(t.data_ptr()) if t is not None else None
 

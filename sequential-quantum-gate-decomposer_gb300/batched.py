@@ -59,6 +59,7 @@ class BatchedDecomposer:
         calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
         self.iters = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
         lib = _native.lib()
+        dev.after_current(stream)
         if self.optimizer == "ADAM":
             _native.check(lib.sqg_decompose_batched_adam(
                 self.native.handle, dev.ptr(t), cols, B, self.trace_offset, self.cost_variant, dev.ptr(x),
@@ -100,6 +101,7 @@ def adam_decompose_graph(circuit, target_udag, x0, tolerance=1e-8, max_iters=100
     lib = _native.lib()
     cols = int(t.shape[1])
     ws = (workspace or dev.Workspace()).get(lib.sqg_adam_loop_workspace_bytes(native.handle, cols))
+    dev.after_current(stream)
     cur = np.finfo(np.float64).max if current_minimum is None or not np.isfinite(current_minimum) else current_minimum
     _native.check(lib.sqg_decompose_adam_loop(
         native.handle, dev.ptr(t), cols, int(trace_offset), int(cost_variant), dev.ptr(x), dev.ptr(cost),
@@ -133,6 +135,7 @@ def bfgs_decompose_graph(circuit, target_udag, x0, tolerance=1e-8, max_calls=100
     lib = _native.lib()
     cols = int(t.shape[1])
     ws = (workspace or dev.Workspace()).get(lib.sqg_bfgs_loop_workspace_bytes(native.handle, cols))
+    dev.after_current(stream)
     _native.check(lib.sqg_decompose_bfgs_loop(
         native.handle, dev.ptr(t), cols, int(trace_offset), int(cost_variant), dev.ptr(x), dev.ptr(cost),
         dev.ptr(calls), dev.ptr(iters), float(tolerance), int(max_calls), int(max_outer), int(iteration_loops),

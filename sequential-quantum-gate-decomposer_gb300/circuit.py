@@ -340,6 +340,7 @@ class Circuit:
             raise ValueError("matrix must be contiguous")
         ws_bytes = _native.lib().sqg_apply_workspace_bytes(nc.handle, B)
         ws = self._ws.get(ws_bytes)
+        dev.after_current(stream)
         _native.check(_native.lib().sqg_apply(nc.handle, dev.ptr(params_dev) if params_dev.numel() else None, B,
                                               dev.ptr(mtx_dev), cols, cols, rows * cols, 1 if fused else 0,
                                               dev.ptr(ws), ws.numel(), dev.stream_ptr(stream)), "sqg_apply")
@@ -356,6 +357,7 @@ class Circuit:
             raise ValueError("state must be contiguous")
         lib = _native.lib()
         ws = self._ws.get(lib.sqg_state_workspace_bytes(nc.handle, B))
+        dev.after_current(stream)
         _native.check(lib.sqg_apply_state(nc.handle, dev.ptr(params_dev) if params_dev.numel() else None, B,
                                           dev.ptr(states_dev), states_dev.shape[-1], 1 if fused else 0, dev.ptr(ws),
                                           ws.numel(), dev.stream_ptr(stream)), "sqg_apply_state")

@@ -76,6 +76,7 @@ class CostEvaluator:
         ws_bytes = self.workspace_bytes(B, with_grad and P > 0, checkpoint_interval)
         ws = self._ws.get(ws_bytes)
         tstride = self.target.shape[-2] * self.target.shape[-1] if self.per_instance else 0
+        dev.after_current(stream)
         _native.check(_native.lib().sqg_cost_grad(
             self.native.handle, dev.ptr(th) if P else None, B, dev.ptr(self.target), self.cols, tstride,
             self.trace_offset, self.variant, dev.ptr(cost), dev.ptr(grad) if (with_grad and P) else None,

@@ -71,6 +71,7 @@ class RaggedBatch:
         return [flat[self.theta_off[i]:self.theta_off[i + 1]] for i in range(self.count)]
 
     def _launch(self, theta_flat, variant, with_grad, stream=None):
+        dev.after_current(stream)
         _native.check(_native.lib().sqg_ragged_cost_grad(
             self.handle, dev.ptr(theta_flat) if self.param_total else None, dev.ptr(self.targets), int(variant),
             dev.ptr(self.cost), dev.ptr(self.grad) if with_grad else None, dev.ptr(self.ws), self.ws.numel(),

@@ -188,6 +188,7 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
         cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
         calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
         w = dev.Workspace().get(lib.sqg_decompose_structures_workspace_bytes(nc.handle, B, target.shape[1]))
+        dev.after_current(stream)  # the start points and the target were copied on the current stream
         _native.check(lib.sqg_decompose_structures(
             nc.handle, recs.ctypes.data, dev.ptr(target), 0, target.shape[1], B, self.trace_offset,
             self.cost_variant, dev.ptr(x), dev.ptr(cost), dev.ptr(calls), None, tol, max_inner, max_outer, loops, 0,
