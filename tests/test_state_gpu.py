@@ -100,3 +100,37 @@ def test_partitioned_circuit_state_matches_oracle(sqg, wl, n, gates, mq):
     torch.cuda.synchronize()
     assert float(np.abs(d.cpu().numpy() - ref).max()) < 1e-12
     assert 1 <= pc.state_block_count() <= len(parts)
+
+
+def test_qasm_program_partitioned_and_simulated(sqg, wl):
+    """The reference's simulation flow: an OpenQASM program, partitioned (Kahn), applied to a
+    state with fused passes that break only at partition boundaries, against the oracle applying
+    the unpartitioned program; and the partition hand-over rejects malformed boundaries."""
+    qasm = importlib.import_module("sequential-quantum-gate-decomposer_gb300.qasm")
+    lib = importlib.import_module("sequential-quantum-gate-decomposer_gb300._native")
+    rng = np.random.default_rng(17)
+    n = 13
+    lines = ["OPENQASM 2.0;", 'include "qelib1.inc";', "qreg q[%d];" % n]
+    for _ in range(300):
+        a, b = (int(v) for v in rng.permutation(n)[:2])
+        lines.append(["h q[%d];" % a, "cx q[%d],q[%d];" % (a, b), "rz(%r) q[%d];" % (float(rng.uniform(-3, 3)), a),
+                      "cz q[%d],q[%d];" % (a, b), "u3(0.3,%r,0.1) q[%d];" % (float(rng.uniform(-3, 3)), a),
+                      "cry(%r) q[%d],q[%d];" % (float(rng.uniform(-3, 3)), a, b)][rng.integers(6)])
+    text = "\n".join(lines)
+    circ, params, phase = qasm.qasm_to_circuit(text)
+    assert phase == 0.0
+    pc, pparams, parts = qasm.PartitionCircuitQasm(text, 5)
+    psi = random_state(n, rng)
+    ref = O.apply_to(n, circ.gate_records(), params, psi.reshape(-1, 1).copy()).reshape(-1)
+    d = torch.from_numpy(psi.copy()).cuda()
+    pc.apply_state_device(torch.from_numpy(pparams).cuda(), d)
+    torch.cuda.synchronize()
+    assert float(np.abs(d.cpu().numpy() - ref).max()) < 1e-12
+    assert pc.state_block_count() <= len(parts)
+    h = circ.native().handle
+    L = circ.get_Gate_Num()
+    for ends in ([L - 1], [5, 3, L], [L + 1]):
+        arr = np.asarray(ends, dtype=np.int32)
+        assert lib.lib().sqg_circuit_set_partitions(h, arr.ctypes.data, arr.size) == 1  # invalid argument
+    arr = np.asarray([], dtype=np.int32)
+    assert lib.lib().sqg_circuit_set_partitions(h, None, 0) == 0  # back to the gate-order plan
