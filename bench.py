@@ -745,6 +745,29 @@ def profile_case(case, profile_calls=60):
         T = np.ascontiguousarray(wl.haar_unitary(64, rng).conj().T)
         batched.bfgs_decompose_graph(c, T, rng.uniform(0, 2 * np.pi, P), max_calls=profile_calls, max_outer=1,
                                      stop_at_tolerance=False)
+    elif case == "state_vector":  # n = 24 simulation circuit, one level: fused blocks, then one pass per gate
+        c = wl.qc_sim_circuit(24, levels=1)
+        th = torch.from_numpy(rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())).cuda()
+        v = torch.randn(1 << 24, dtype=torch.complex128, device="cuda")
+        c.apply_state_device(th, v, fused=True)
+        c.apply_state_device(th, v, fused=False)
+    elif case == "env_costgrad":  # small-register cost + gradient, 4096 parameter vectors of the 3-qubit ansatz
+        ansatz, targets = make_workload(sqg, wl)
+        P = ansatz.get_Parameter_Num()
+        ev = sqg.CostEvaluator(ansatz, torch.from_numpy(targets).cuda())
+        ev.cost_grad(torch.from_numpy(rng.uniform(0, 2 * np.pi, (targets.shape[0], P))).cuda())
+    elif case == "ragged":  # uneven batch: 128 instances, n ~ U{3..9}
+        rg = importlib.import_module(PKG + ".ragged")
+        circs, tg, ths = [], [], []
+        for _ in range(128):
+            n = int(rng.integers(3, 10))
+            c = wl.cnot_u3_ansatz(n, 3 * n * (n - 1) // 2)
+            P = c.get_Parameter_Num()
+            circs.append(c)
+            tg.append(np.ascontiguousarray(c.get_Matrix(rng.uniform(0, 2 * np.pi, P)).conj().T))
+            ths.append(rng.uniform(0, 2 * np.pi, P))
+        rb = rg.RaggedBatch(circs, tg)
+        rb.cost_grad(rb.pack(ths))
     elif case == "cost_grad":
         c = wl.cnot_u3_ansatz(8, 60)
         P = c.get_Parameter_Num()
@@ -758,7 +781,8 @@ def profile_case(case, profile_calls=60):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe-fp64", action="store_true", help="print the live FP64 FMA peak by active lanes")
-    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad", "mlp_gemm", "dropin_bfgs_n6"],
+    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad", "mlp_gemm", "dropin_bfgs_n6",
+                                                     "state_vector", "env_costgrad", "ragged"],
                     default=None)
     ap.add_argument("--profile-calls", type=int, default=60,
                     help="evaluations per BFGS run in the decompose profile case (below 60: no tolerance stop)")
