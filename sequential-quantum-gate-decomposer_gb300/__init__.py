@@ -21,13 +21,14 @@ from .evaluator import (FROBENIUS_NORM, HILBERT_SCHMIDT_TEST, INFIDELITY, Circui
                         circuit_cost)
 from .partitioning import PartitionCircuit
 from .qasm import CompareCircuits, PartitionCircuitQasm, qasm_to_circuit, qasm_to_squander_circuit
-from .adaptive import N_Qubit_Decomposition_adaptive
+from .adaptive import N_Qubit_Decomposition_adaptive, N_Qubit_State_Preparation_adaptive
 from .tree_search import N_Qubit_Decomposition_Tabu_Search, N_Qubit_Decomposition_Tree_Search
 
 _sys.modules.setdefault("sqg_gb300", _sys.modules[__name__])
 
 __all__ = ["Circuit", "BatchedDecomposer", "N_Qubit_Decomposition_custom", "N_Qubit_Decomposition_Tree_Search",
            "N_Qubit_Decomposition_Tabu_Search", "N_Qubit_Decomposition_adaptive",
+           "N_Qubit_State_Preparation_adaptive",
            "PartitionCircuit", "PartitionCircuitQasm", "qasm_to_circuit", "qasm_to_squander_circuit", "CompareCircuits", "CostEvaluator", "CircuitCost", "circuit_cost", "SQGError",
            "build", "FROBENIUS_NORM", "HILBERT_SCHMIDT_TEST", "INFIDELITY", "U3", "RX", "RY", "RZ", "CNOT", "CZ",
            "CRY"]

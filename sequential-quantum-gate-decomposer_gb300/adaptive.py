@@ -406,3 +406,27 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
         self.optimized_parameters = x
         self.decomposition_error = self.Optimization_Problem(x)
         return 0
+
+
+class N_Qubit_State_Preparation_adaptive(N_Qubit_Decomposition_adaptive):
+    """Drop-in for squander.N_Qubit_State_Preparation_adaptive(State, level_limit_max=8,
+    level_limit_min=0, topology=None, config={})
+    (squander/decomposition/qgd_N_Qubit_State_Preparation_adaptive.py): the adaptive decomposition
+    of a state given as a complex128 column vector, so that the circuit maps it to |0...0>
+    (the cost 1 - Re (C psi)_0 of a one-column target)."""
+
+    def __init__(self, State, level_limit_max=8, level_limit_min=0, topology=None, config=None):
+        if not isinstance(State, np.ndarray):
+            raise Exception("Initial state should be a numpy array")
+        if State.dtype != np.complex128:
+            raise Exception("Initial state should be made of complex values")
+        if not State.flags.c_contiguous:
+            raise Exception("Initial state should be contiguous in memory")
+        if State.ndim == 1:
+            State = State.reshape((State.size, 1))
+        if not (State.ndim == 2 and State.shape[1] == 1):
+            raise Exception("Initial state not properly formatted. Input state must be a column vector")
+        super().__init__(State, -1, level_limit_max, level_limit_min, topology=topology, config=config)
+
+    def get_Qiskit_Circuit(self):
+        raise NotImplementedError("Qiskit is not part of this engine")

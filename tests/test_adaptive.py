@@ -92,3 +92,29 @@ def test_adaptive_decomposition_reaches_tolerance(sqg, ad, n, blocks):
     assert abs(abs(np.trace(C @ T)) / (1 << n) - 1.0) < 1e-8  # up to the global phase moved onto the target
     gates = dec.get_Circuit().get_Gate_Nums()
     assert gates.get("CRY", 0) == 0  # finalised into CNOT / CZ constructions
+
+
+def test_state_preparation_input_checks(sqg):
+    with pytest.raises(Exception, match="numpy array"):
+        sqg.N_Qubit_State_Preparation_adaptive([1, 0])
+    with pytest.raises(Exception, match="complex"):
+        sqg.N_Qubit_State_Preparation_adaptive(np.zeros(4))
+    with pytest.raises(Exception, match="column vector"):
+        sqg.N_Qubit_State_Preparation_adaptive(np.zeros((4, 2), dtype=np.complex128))
+    sp = sqg.N_Qubit_State_Preparation_adaptive(np.ones(8, dtype=np.complex128) / np.sqrt(8), 3)
+    assert sp.qbit_num == 3 and sp.level_limit == 3 and sp.get_Unitary().shape == (8, 1)
+
+
+@pytest.mark.gpu
+def test_state_preparation_maps_the_state_to_zero(sqg):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(8)
+    psi = rng.standard_normal(8) + 1j * rng.standard_normal(8)
+    psi = np.ascontiguousarray(psi / np.linalg.norm(psi))
+    sp = sqg.N_Qubit_State_Preparation_adaptive(psi, level_limit_max=4, level_limit_min=1,
+                                                config={"optimization_tolerance": 1e-8, "random_seed": 2})
+    sp.Start_Decomposition()
+    torch.cuda.synchronize()
+    assert sp.get_Decomposition_Error() < 1e-8
+    C = O.get_matrix(3, sp.get_Circuit().gate_records(), sp.get_Optimized_Parameters())
+    assert abs(abs((C @ psi)[0]) - 1.0) < 1e-8
