@@ -148,6 +148,11 @@ class Circuit:
     def add_CRY(self, target_qbit, control_qbit):
         self._add(CRY, target_qbit, control_qbit)
 
+    def add_adaptive(self, target_qbit, control_qbit):
+        """The adaptive controlled rotation of the adaptive decomposer: a CRY, its activation
+        function being the identity (src-cpp/common/common.cpp:35-38)."""
+        self._add(CRY, target_qbit, control_qbit)
+
     def add_Circuit(self, other):
         """Append a sub-circuit as one block (Gates_block::add_gate of a nested block, its
         parameters contiguous after the ones before it)."""
@@ -362,6 +367,45 @@ class Circuit:
                                           dev.ptr(states_dev), states_dev.shape[-1], 1 if fused else 0, dev.ptr(ws),
                                           ws.numel(), dev.stream_ptr(stream)), "sqg_apply_state")
         return states_dev
+
+    def get_Second_Renyi_Entropy(self, parameters=None, input_state=None, qubit_list=None):
+        """Second Renyi entropy -log Tr(rho^2) of the reduced density matrix of qubit_list (all
+        qubits when None) of the circuit's output state for input_state (|0...0> when None)
+        (qgd_Circuit.get_Second_Renyi_Entropy, Gates_block::get_second_Renyi_entropy,
+        src-cpp/gates/Gates_block.cpp:3625-3650).  The state is transformed on the GPU; the
+        purity is one matrix product of the state reshaped as (kept qubits) x (traced qubits)."""
+        n = self.qbit_num
+        if isinstance(qubit_list, (list, tuple)):
+            if not all(isinstance(q, (int, np.integer)) for q in qubit_list):
+                print("Elements of qbit_list should be integers")
+                return None
+            keep = sorted(set(int(q) for q in qubit_list))
+        elif qubit_list is None:
+            keep = list(range(n))
+        else:
+            print("Elements of qbit_list should be integers")
+            return None
+        if parameters is None:
+            print("get_Second_Renyi_entropy: array of input parameters is None")
+            return None
+        if any(not 0 <= q < n for q in keep):
+            raise ValueError("qubit index out of range")
+        if input_state is None:
+            psi = np.zeros(1 << n, dtype=np.complex128)
+            psi[0] = 1.0
+        else:
+            psi = np.ascontiguousarray(np.asarray(input_state, dtype=np.complex128).reshape(-1))
+            if psi.size != (1 << n):
+                raise ValueError("input state must have 2**qbit_num amplitudes")
+        torch = dev.torch
+        v = dev.to_device_complex(psi)
+        self.apply_state_device(self._params_dev(parameters), v)
+        traced = [q for q in range(n) if q not in keep]
+        axes = [n - 1 - q for q in keep] + [n - 1 - q for q in traced]  # amplitude index bit q = axis n-1-q
+        M = v.reshape([2] * n).permute(axes).reshape(1 << len(keep), 1 << len(traced))
+        rho = M @ M.conj().transpose(0, 1) if len(keep) <= len(traced) else M.conj().transpose(0, 1) @ M
+        purity = float((rho.real * rho.real + rho.imag * rho.imag).sum().item())
+        return -float(np.log(purity))
 
     def state_block_count(self):
         """Fused passes over a state vector (blocks of the state-vector plan)."""

@@ -134,3 +134,29 @@ def test_qasm_program_partitioned_and_simulated(sqg, wl):
         assert lib.lib().sqg_circuit_set_partitions(h, arr.ctypes.data, arr.size) == 1  # invalid argument
     arr = np.asarray([], dtype=np.int32)
     assert lib.lib().sqg_circuit_set_partitions(h, None, 0) == 0  # back to the gate-order plan
+
+
+def test_second_renyi_entropy(sqg, wl):
+    """Bell pair: S2 of one qubit is log 2; a product state has S2 = 0; against a direct numpy
+    reduced density matrix of a random 10-qubit circuit's output."""
+    c = sqg.Circuit(3)
+    c.add_U3(0)            # H = U3(pi/2, 0, pi): stored (pi/4, 0, pi)
+    c.add_CNOT(1, 0)
+    c.add_adaptive(2, 1)   # a CRY at angle 0: the identity
+    p = np.array([np.pi / 4, 0.0, np.pi, 0.0])
+    assert np.isclose(c.get_Second_Renyi_Entropy(p, qubit_list=[0]), np.log(2), atol=1e-12)
+    assert np.isclose(c.get_Second_Renyi_Entropy(p, qubit_list=[2]), 0.0, atol=1e-12)
+    assert np.isclose(c.get_Second_Renyi_Entropy(p), 0.0, atol=1e-12)
+    assert c.get_Second_Renyi_Entropy(None) is None
+    rng = np.random.default_rng(33)
+    n = 10
+    c = wl.all_gates_circuit(n, 120, rng)
+    th = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    psi = random_state(n, rng)
+    out = O.apply_to(n, c.gate_records(), th, psi.reshape(-1, 1).copy()).reshape(-1)
+    keep = [1, 4, 7, 8]
+    t = out.reshape([2] * n).transpose([n - 1 - q for q in keep] + [n - 1 - q for q in range(n) if q not in keep])
+    M = t.reshape(1 << len(keep), -1)
+    rho = M @ M.conj().T
+    want = -np.log(np.sum(np.abs(rho) ** 2))
+    assert np.isclose(c.get_Second_Renyi_Entropy(th, psi, keep), want, atol=1e-10)
