@@ -164,3 +164,60 @@ def test_tabu_search_reaches_tolerance(sqg, ts):
     assert dec.structures_tested >= 2
     x = dec.get_Optimized_Parameters()
     assert abs(O.cost(n, dec.get_Circuit().gate_records(), x, dec.get_Unitary())) < 1e-8
+
+
+@pytest.mark.gpu
+def test_structures_with_per_instance_targets(sqg, ts):
+    """target_stride > 0: instance k decomposes its own target; equal to a one-structure batch."""
+    torch = pytest.importorskip("torch")
+    lib = importlib.import_module("sequential-quantum-gate-decomposer_gb300._native")
+    topo = ts.normalize_topology(None, 3)
+    codes = ts.level_codes(2, topo)[[0, 3, 7]]
+    B = codes.shape[0]
+    rng = np.random.default_rng(12)
+    xs = rng.uniform(0, 2 * np.pi, (B, 21))
+    T = np.stack([np.ascontiguousarray(O.get_matrix(3, ts.structure_circuit(codes[k], topo, 3).gate_records(),
+                                                     xs[k]).conj().T) for k in range(B)])
+    x0 = xs + 0.1 * rng.standard_normal(xs.shape)
+    nc = ts.structure_circuit(codes[0], topo, 3).native()
+    recs = np.ascontiguousarray(ts.structure_records(codes, topo, 3))
+    t = torch.from_numpy(T).cuda()
+    x = torch.from_numpy(x0.copy()).cuda()
+    cost = torch.empty(B, dtype=torch.float64, device="cuda")
+    calls = torch.empty(B, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.lib().sqg_decompose_structures_workspace_bytes(nc.handle, B, 8), dtype=torch.uint8,
+                     device="cuda")
+    lib.check(lib.lib().sqg_decompose_structures(nc.handle, recs.ctypes.data, t.data_ptr(), 64, 8, B, 0, 0,
+                                                 x.data_ptr(), cost.data_ptr(), calls.data_ptr(), None, 1e-8, 1000,
+                                                 4, 1, 1, 5, ws.data_ptr(), ws.numel(),
+                                                 torch.cuda.current_stream().cuda_stream), "structures")
+    torch.cuda.synchronize()
+    assert np.all(cost.cpu().numpy() < 1e-8)
+    for k in range(B):
+        dec = sqg.BatchedDecomposer(ts.structure_circuit(codes[k], topo, 3), tolerance=1e-8, max_calls=1000,
+                                    max_outer=4)
+        xk, ck, nk = dec.run(T, x0, seed=5)
+        torch.cuda.synchronize()
+        assert float(ck[k]) == float(cost[k]) and torch.equal(xk[k], x[k])
+    with pytest.raises(lib.SQGError, match="target stride"):
+        lib.check(lib.lib().sqg_decompose_structures(nc.handle, recs.ctypes.data, t.data_ptr(), 10, 8, B, 0, 0,
+                                                     x.data_ptr(), cost.data_ptr(), calls.data_ptr(), None, 1e-8,
+                                                     10, 1, 1, 1, 0, ws.data_ptr(), ws.numel(),
+                                                     torch.cuda.current_stream().cuda_stream), "structures")
+
+
+@pytest.mark.gpu
+def test_tree_search_on_a_linear_topology(sqg, ts):
+    """Four qubits on a line (0-1, 1-2, 2-3): commuting CNOTs on disjoint pairs are enumerated
+    once; a target from two such CNOTs is found at level 2."""
+    topo = ts.normalize_topology([(0, 1), (1, 2), (2, 3)], 4)
+    code = [0, 2]  # (0,1) then (2,3): canonical
+    c = ts.structure_circuit(code, topo, 4)
+    rng = np.random.default_rng(3)
+    U = O.get_matrix(4, c.gate_records(), rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
+    dec = sqg.N_Qubit_Decomposition_Tree_Search(np.ascontiguousarray(U.conj().T), topology=[(0, 1), (1, 2), (2, 3)],
+                                                config={"optimization_tolerance": 1e-8, "random_seed": 2})
+    dec.Start_Decomposition()
+    assert dec.get_Decomposition_Error() < 1e-8
+    assert len(dec.best_cnot_sequence) <= 2
+    assert all(p in topo for p in dec.best_cnot_sequence)
