@@ -172,17 +172,19 @@ def test_graph_bfgs_equals_k_decompose(sqg, wl, batched, n, blocks, max_outer, l
     assert int(ng.item()) >= max_outer * loops
 
 
-@pytest.mark.parametrize("n,blocks", [(6, 4), (6, 25)])
-def test_graph_bfgs_above_five_qubits_follows_host_bfgs(sqg, wl, batched, n, blocks):
-    """Tile-kernel evaluation in the graph body (P = 42 on 64 threads, P = 168 on 256): one BFGS
-    run follows the host-driven BFGS_Powell restatement over the same cost and gradient."""
+@pytest.mark.parametrize("n,blocks,cols,offset", [(6, 4, 64, 0), (6, 25, 64, 0), (7, 6, 48, 64)])
+def test_graph_bfgs_above_five_qubits_follows_host_bfgs(sqg, wl, batched, n, blocks, cols, offset):
+    """Tile-kernel evaluation in the graph body (P = 42 on 64 threads, P = 168 on 256, and a
+    rectangular target with a trace offset): one BFGS run follows the host-driven BFGS_Powell
+    restatement over the same cost and gradient."""
     optim = importlib.import_module("sequential-quantum-gate-decomposer_gb300.optim")
     rng = np.random.default_rng(600 + blocks)
     c = wl.cnot_u3_ansatz(n, blocks)
     P = c.get_Parameter_Num()
-    T = np.ascontiguousarray(O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, P)).conj().T)
+    T = O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, P)).conj().T
+    T = np.ascontiguousarray(T[:, offset:offset + cols])
     x0 = rng.uniform(0, 2 * np.pi, P)
-    ev = sqg.CostEvaluator(c, T)
+    ev = sqg.CostEvaluator(c, T, trace_offset=offset)
 
     def fg(x):
         cost, grad = ev.cost_grad(torch.from_numpy(x).cuda())
@@ -191,7 +193,7 @@ def test_graph_bfgs_above_five_qubits_follows_host_bfgs(sqg, wl, batched, n, blo
     xh = x0.copy()
     fh, nh = optim.bfgs_powell(fg, xh, 40)
     xg, cg, ng, _ = batched.bfgs_decompose_graph(c, T, x0, max_calls=40, max_outer=1, iteration_loops=1,
-                                                 stop_at_tolerance=False, seed=1)
+                                                 stop_at_tolerance=False, seed=1, trace_offset=offset)
     torch.cuda.synchronize()
     assert int(ng.item()) == nh
     assert np.isclose(float(cg.item()), fh, rtol=1e-7, atol=1e-12)
