@@ -187,6 +187,8 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
     def _initial(self, tol):
         """determine_initial_gate_structure: levels level_limit_min..level_limit of adaptive
         layers plus the final layer, each decomposed from a random start; the best one wins."""
+        if self.level_limit_min > self.level_limit:
+            raise ValueError("level_limit_min exceeds level_limit_max: no circuit to optimize")
         results = []
         level = self.level_limit_min
         while level <= self.level_limit:

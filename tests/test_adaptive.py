@@ -72,6 +72,9 @@ def test_penalty_and_parameter_bookkeeping(sqg, ad):
     assert r.size == s.param_num() - 7 and r[6] == 6 and r[7] == 14
     layer = d._adaptive_layer()
     assert [(b[0][1], b[1][1]) for b in layer] == [(0, 1), (0, 2), (1, 2)]
+    bad = ad.N_Qubit_Decomposition_adaptive(np.eye(8, dtype=np.complex128), level_limit_max=1, level_limit_min=2)
+    with pytest.raises(ValueError, match="level_limit_min"):
+        bad._initial(1e-8)
 
 
 @pytest.mark.gpu
