@@ -197,8 +197,9 @@ int sqg_apply_from_right(const sqg_circuit* circuit, const double* theta_dev, vo
 int sqg_combined_unitary(const sqg_circuit* circuit, const double* theta_dev, const void* target_dev, int cols,
                          void* out_dev, void* workspace_dev, size_t workspace_bytes, void* stream);
 
-/* Batched decomposition of `batch` small targets (qbit_num <= 5), one complete BFGS
- * decomposition per CTA, entirely on the device.
+/* Batched decomposition of `batch` small targets (qbit_num <= 6, the instance's shared memory
+ * within the device's per-CTA limit), one complete BFGS decomposition per CTA, entirely on
+ * the device.
  *   targets_dev  batch x rows x cols complex128 (each U^dagger);
  *   x_dev        batch x P doubles: start points in, best parameters out;
  *   cost_dev     batch doubles out (best cost);  calls_dev  batch ints out (cost+gradient
@@ -259,7 +260,7 @@ int sqg_decompose_structures(const sqg_circuit* circuit, const sqg_gate* gates, 
  * (src-cpp/common/Adam.cpp: beta1 0.68, beta2 0.8, epsilon 1e-4, local-minimum test) and
  * randomize_parameters (src-cpp/decomposition/Optimization_Interface.cpp:576-607), the
  * optimizer N_Qubit_Decomposition_custom selects above five qubits
- * (N_Qubit_Decomposition_custom.cpp:59-76), here for qbit_num <= 5 with one CTA per target.
+ * (N_Qubit_Decomposition_custom.cpp:59-76), here for qbit_num <= 6 with one CTA per target.
  * Each target runs up to max_outer engine calls of at most max_iters cost+gradient
  * evaluations (learning rate eta, adaptive as in the reference when adaptive_eta != 0, at
  * most random_shift_count_max randomisations, randomisation after randomization_threshold

@@ -49,6 +49,7 @@ struct DecArgs {
   double* zglob;
   int z_in_smem;
   int cyclic;  // cost and gradient through the environment matrix (dec_eval_cyclic)
+  int has_lam;  // 0: the one-chain environment form of a square target, which needs no lambda tiles
   int chains;  // 2: the two-warp form dec_eval_cyclic2, split at gate `split`
   int split;
   // ADAM engine (k_decompose<kAdam>)
@@ -238,7 +239,7 @@ __device__ __forceinline__ void cyclic_overlap(const double2* m, int n, int N, c
 __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* xv, double* gv, int b) {
   const int n = a.n, N = a.N, NN = N * N, cols = a.cols, off = a.trace_offset, L = a.L;
   dec_build(a, sh, xv);
-  double2* m = sh.psi;  // psi and lam are contiguous and hold >= N * N entries
+  double2* m = sh.psi;  // N * N entries: psi alone when cols = N, else psi and the contiguous lam
   const double2* T = sh.tgt;
   for (int e = threadIdx.x; e < NN; e += blockDim.x) {
     const int c = e >> n, r = e & (N - 1), j = c - off;
@@ -268,7 +269,11 @@ __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* 
       if (g == 0 && threadIdx.x < 32) {
         const int lane = threadIdx.x;
         double2 v = lane < N ? m[lane * N + lane] : make_double2(0.0, 0.0);
-        for (int o = 1; o < N; o <<= 1) {  // lanes 0..N-1 end with the full sum
+        for (int i = lane + 32; i < N; i += 32) {  // N = 64: two diagonal entries per lane
+          v.x += m[i * N + i].x;
+          v.y += m[i * N + i].y;
+        }
+        for (int o = 1; o < min(N, 32); o <<= 1) {  // lanes 0..min(N, 32)-1 end with the full sum
           v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
           v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
         }
@@ -555,7 +560,7 @@ __device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
   double2* tsh = (double2*)take(sizeof(double2) * NC);
   sh.tgt = tsh;
   sh.psi = (double2*)take(sizeof(double2) * NC);
-  sh.lam = (double2*)take(sizeof(double2) * NC);
+  sh.lam = a.has_lam ? (double2*)take(sizeof(double2) * NC) : nullptr;
   sh.gm = (GateMat*)take(sizeof(GateMat) * max(L, 1));
   sh.sc = (double2*)take(sizeof(double2) * max(P, 1));
   sh.R = (double*)take(sizeof(double) * 8 * max(L, 1));
@@ -678,10 +683,21 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   }
 }
 
+bool use_cyclic(const sqg_circuit* c, int cols);
+bool use_two_chains();
+
+// The lambda tiles are needed by every evaluation form except the one-chain environment form
+// of a square target, whose environment matrix (N * N entries) fits in the psi tiles.
+bool dec_needs_lam(const sqg_circuit* c, int cols) {
+  if (!use_cyclic(c, cols) || cols != c->N) return true;
+  return c->N * c->N / 2 <= 32 && c->L >= 2 && use_two_chains();
+}
+
 size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem, bool adam = false) {
   auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
-  size_t s = r16(sizeof(Gate) * L) + 3 * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
+  const size_t tiles = dec_needs_lam(c, cols) ? 3 : 2;  // target, psi (and lambda)
+  size_t s = r16(sizeof(Gate) * L) + tiles * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
              r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) + r16(sizeof(int) * L) +
              kDecVectors * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
              r16(sizeof(double) * kTileMaxWarps);
@@ -775,6 +791,7 @@ int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, v
 
 // Evaluation form of the decomposition kernels for this circuit and target width.
 void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
+  a.has_lam = dec_needs_lam(c, cols) ? 1 : 0;
   a.inv_cols = 1.0 / cols;
   a.cyclic = use_cyclic(c, cols) ? 1 : 0;
   a.chains = 1;
@@ -850,7 +867,7 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
     return set_error(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
   const int off = cost_variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
   if (off < 0 || off + cols > c->N) return set_error(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
-  if (c->n > 5) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 5");
+  if (c->n > 6) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 6");
   if (max_calls < 1 || max_outer < 1 || iteration_loops < 1)
     return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
   const bool zs = z_in_shared(c, cols);
@@ -897,7 +914,7 @@ int sqg_decompose_structures(const sqg_circuit* c, const sqg_gate* gates, const 
     return set_error(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
   const int off = cost_variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
   if (off < 0 || off + cols > c->N) return set_error(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
-  if (c->n > 5) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 5");
+  if (c->n > 6) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 6");
   if (max_calls < 1 || max_outer < 1 || iteration_loops < 1)
     return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
   if (target_stride != 0 && target_stride < (long long)c->N * cols)
@@ -963,7 +980,7 @@ int sqg_decompose_batched_adam(const sqg_circuit* c, const void* targets, int co
     return set_error(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
   const int off = cost_variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
   if (off < 0 || off + cols > c->N) return set_error(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
-  if (c->n > 5) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 5");
+  if (c->n > 6) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 6");
   if (max_iters < 1 || max_outer < 1 || random_shift_count_max < 0 || randomization_threshold < 0)
     return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
   const size_t smem = dec_smem_bytes(c, cols, false, true);

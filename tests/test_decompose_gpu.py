@@ -93,10 +93,57 @@ def test_exact_start_stops_after_one_evaluation(sqg, wl):
     assert np.all(cost.cpu().numpy() < 1e-12)
 
 
+@pytest.mark.parametrize("cols,offset,form", [(64, 0, None), (64, 0, "sweep"), (48, 8, None), (16, 4, None)])
+def test_six_qubit_first_bfgs_steps_follow_the_oracle(sqg, wl, monkeypatch, cols, offset, form):
+    """Six qubits (one 64 x 64 target per CTA): the one-chain environment form keeps the
+    4096-entry environment matrix in the psi tiles alone (no lambda tiles), rectangular
+    targets keep both; the state sweeps cover narrow targets."""
+    if form:
+        monkeypatch.setenv("SQG_DECOMPOSE_FORM", form)
+    n = 6
+    rng = np.random.default_rng(80 + cols + offset)
+    c = wl.cnot_u3_ansatz(n, 3)
+    P = c.get_Parameter_Num()
+    recs = c.gate_records()
+    B = 3
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, recs, rng.uniform(0, 2 * np.pi, P)).conj().T[:, offset:offset + cols])
+                        for _ in range(B)])
+    x0 = rng.uniform(0, 2 * np.pi, (B, P))
+    dec = sqg.BatchedDecomposer(c, tolerance=0.0, max_calls=5, max_outer=1, stop_at_tolerance=False, trace_offset=offset)
+    x, cost, calls = dec.run(targets, x0)
+    torch.cuda.synchronize()
+    xr, cr, callr = O.decompose(n, recs, targets, x0, tolerance=0.0, max_inner=5, max_outer=1, trace_offset=offset)
+    assert np.array_equal(calls.cpu().numpy(), callr)
+    assert np.allclose(cost.cpu().numpy(), cr, rtol=1e-9, atol=1e-12)
+    assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)
+
+
+def test_six_qubit_exact_start_and_restart(sqg, wl):
+    """Six-qubit targets built by the circuit: an exact start stops after one evaluation, a
+    perturbed one converges below the tolerance (checked by the oracle's cost)."""
+    n = 6
+    rng = np.random.default_rng(81)
+    c = wl.cnot_u3_ansatz(n, 2)
+    P = c.get_Parameter_Num()
+    recs = c.gate_records()
+    p = rng.uniform(0, 2 * np.pi, (4, P))
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, recs, p[b]).conj().T) for b in range(4)])
+    x, cost, calls = sqg.BatchedDecomposer(c).run(targets, p)
+    torch.cuda.synchronize()
+    assert np.all(calls.cpu().numpy() == 1) and np.all(cost.cpu().numpy() < 1e-12)
+    x0 = p + rng.normal(0.0, 0.05, p.shape)
+    x, cost, calls = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=2000, max_outer=2).run(targets, x0)
+    torch.cuda.synchronize()
+    xs, cs = x.cpu().numpy(), cost.cpu().numpy()
+    assert np.all(cs < 1e-8), cs
+    for b in range(4):
+        assert O.cost(n, recs, xs[b], targets[b]) < 1e-8
+
+
 def test_rejects_unsupported(sqg, wl):
-    c = wl.cnot_u3_ansatz(6, 2)
+    c = wl.cnot_u3_ansatz(7, 1)
     with pytest.raises(Exception):
-        sqg.BatchedDecomposer(c).run(np.zeros((1, 64, 64), dtype=np.complex128), np.zeros((1, c.get_Parameter_Num())))
+        sqg.BatchedDecomposer(c).run(np.zeros((1, 128, 128), dtype=np.complex128), np.zeros((1, c.get_Parameter_Num())))
 
 
 def test_every_restart_gets_its_own_budget(sqg, wl):
