@@ -319,6 +319,7 @@ def bench_ours(args):
         line["cost_grad_n10"] = bench_cost_grad_n10(sqg, wl, torch)
         line["decompose_n4_single"] = bench_single_n4(sqg, wl, torch)
         line["dropin_loops"] = bench_dropin_loops(sqg, wl, torch)
+        line["decompose_n6_batched"] = bench_decompose_n6(sqg, wl, torch)
         line["state_vector_n24"] = bench_state_vector(sqg, wl, torch)
         line["decompose_16384_one_launch"] = bench_large_batch(sqg, wl, torch, ansatz, targets)
     if not args.skip_cpu:
@@ -554,6 +555,32 @@ def bench_dropin_loops(sqg, wl, torch):
                              "seconds": dt, "levels": d.levels_done, "structures": cand,
                              "structures_per_s": cand / dt, "cnots_found": len(d.best_cnot_sequence),
                              "error": d.get_Decomposition_Error()}
+    return out
+
+
+def bench_decompose_n6(sqg, wl, torch):
+    """Batched six-qubit decompositions, one CTA per target (target read from L2, four warps
+    per CTA): 608 targets built by the ansatz from random parameters, BFGS with one run of at
+    most 500 evaluations from random starts."""
+    out = {}
+    for blocks in (3, 8):
+        rng = np.random.default_rng(5)
+        c = wl.cnot_u3_ansatz(6, blocks)
+        P = c.get_Parameter_Num()
+        B = 608
+        T = np.stack([np.ascontiguousarray(c.get_Matrix(rng.uniform(0, 2 * np.pi, P)).conj().T) for _ in range(B)])
+        tdev = torch.as_tensor(T, device="cuda")
+        x0 = torch.as_tensor(rng.uniform(0, 2 * np.pi, (B, P)), device="cuda")
+        dec = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=500, max_outer=1)
+        dec.run(tdev, x0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, cost, calls = dec.run(tdev, x0)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        ev = int(calls.sum().item())
+        out["P%d" % P] = {"targets": B, "seconds": dt, "decompositions_per_s": B / dt, "evaluations": ev,
+                          "evaluations_per_s": ev / dt, "solved_fraction": float((cost < 1e-8).float().mean().item())}
     return out
 
 

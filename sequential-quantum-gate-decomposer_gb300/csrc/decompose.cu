@@ -50,6 +50,7 @@ struct DecArgs {
   int z_in_smem;
   int cyclic;  // cost and gradient through the environment matrix (dec_eval_cyclic)
   int has_lam;  // 0: the one-chain environment form of a square target, which needs no lambda tiles
+  int tgt_in_smem;  // 1: the target is copied to shared memory; 0: read from global memory (L2)
   int chains;  // 2: the two-warp form dec_eval_cyclic2, split at gate `split`
   int split;
   // ADAM engine (k_decompose<kAdam>)
@@ -63,7 +64,7 @@ enum { kBfgs = 0, kAdam = 1 };
 
 struct Sh {
   const Gate* gates;    // shared-memory copy of the gate list
-  const double2* tgt;  // shared-memory copy of this instance's target (N x cols, row-major)
+  const double2* tgt;  // this instance's target (N x cols, row-major): shared-memory copy or global
   double2 *psi, *lam, *sc;
   GateMat* gm;
   double* R;   // [L][8] reduced 2x2 overlaps of the reverse sweep
@@ -557,8 +558,8 @@ __device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
   auto take = [&](size_t bytes) { char* r = p; p += (bytes + 15) / 16 * 16; return r; };
   Gate* gsh = (Gate*)take(sizeof(Gate) * max(L, 1));
   sh.gates = gsh;
-  double2* tsh = (double2*)take(sizeof(double2) * NC);
-  sh.tgt = tsh;
+  double2* tsh = a.tgt_in_smem ? (double2*)take(sizeof(double2) * NC) : nullptr;
+  sh.tgt = a.tgt_in_smem ? tsh : a.targets + (long long)b * a.tstride;
   sh.psi = (double2*)take(sizeof(double2) * NC);
   sh.lam = a.has_lam ? (double2*)take(sizeof(double2) * NC) : nullptr;
   sh.gm = (GateMat*)take(sizeof(GateMat) * max(L, 1));
@@ -581,7 +582,8 @@ __device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
   sh.tot = (double*)take(sizeof(double) * 8);
   sh.scratch = (double*)take(sizeof(double) * kTileMaxWarps);
   sh.Z = nullptr;
-  for (int e = threadIdx.x; e < NC; e += blockDim.x) tsh[e] = a.targets[(long long)b * a.tstride + e];
+  if (a.tgt_in_smem)
+    for (int e = threadIdx.x; e < NC; e += blockDim.x) tsh[e] = a.targets[(long long)b * a.tstride + e];
   for (int g = threadIdx.x; g < L; g += blockDim.x) {
     const Gate gt = gl[g];
     gsh[g] = gt;
@@ -693,10 +695,24 @@ bool dec_needs_lam(const sqg_circuit* c, int cols) {
   return c->N * c->N / 2 <= 32 && c->L >= 2 && use_two_chains();
 }
 
+// Six-qubit targets (up to 64 KB) stay in global memory: a copy in shared memory would halve the
+// CTAs an SM holds, and the evaluation reads the target once (into the environment matrix or
+// the first state), from L2.
+bool dec_target_in_smem(const sqg_circuit* c) { return c->n <= 5; }
+
+// Threads of a decomposition CTA: one per parameter for the vector and Z-matrix work, at least
+// two warps; four at six qubits, where shared memory admits few CTAs per SM and the
+// evaluation's 2048 amplitude pairs per gate keep every warp busy.
+int dec_threads(const sqg_circuit* c) {
+  if (c->n >= 6) return kDecThreads;
+  return std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
+}
+
 size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem, bool adam = false) {
   auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
-  const size_t tiles = dec_needs_lam(c, cols) ? 3 : 2;  // target, psi (and lambda)
+  // psi, lambda unless the form needs none, the target unless it stays in global memory
+  const size_t tiles = 1 + (dec_needs_lam(c, cols) ? 1 : 0) + (dec_target_in_smem(c) ? 1 : 0);
   size_t s = r16(sizeof(Gate) * L) + tiles * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
              r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) + r16(sizeof(int) * L) +
              kDecVectors * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
@@ -775,9 +791,7 @@ int dec_launch_form(const sqg_circuit* c, const DecArgs& a, int batch, size_t sm
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-  // one thread per parameter for the vector and Z-matrix work, at least two warps
-  const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
-  k_decompose<OPT, FORM><<<batch, threads, smem, (cudaStream_t)stream>>>(a);
+  k_decompose<OPT, FORM><<<batch, dec_threads(c), smem, (cudaStream_t)stream>>>(a);
   e = cudaGetLastError();
   return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
 }
@@ -792,6 +806,7 @@ int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, v
 // Evaluation form of the decomposition kernels for this circuit and target width.
 void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
   a.has_lam = dec_needs_lam(c, cols) ? 1 : 0;
+  a.tgt_in_smem = dec_target_in_smem(c) ? 1 : 0;
   a.inv_cols = 1.0 / cols;
   a.cyclic = use_cyclic(c, cols) ? 1 : 0;
   a.chains = 1;
@@ -839,7 +854,7 @@ int env_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* 
   a.tstride = tstride;
   a.B = B;
   dec_eval_form(c, cols, off, a);
-  const int threads = std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
+  const int threads = dec_threads(c);
   cudaStream_t s = (cudaStream_t)stream;
   if (a.chains == 2) return env_launch<kFormTwoChains>(a, theta, cost, grad, threads, smem, s);
   return env_launch<kFormCyclic>(a, theta, cost, grad, threads, smem, s);
