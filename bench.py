@@ -11,8 +11,8 @@ circuit, batch of 4 parameter vectors, fused vs unfused, HBM GB/s) and the batch
 cost+gradient evaluation at n=8 (B=1024, 360 blocks).
 
 --impl reference times the reference algorithm on the host cores instead (the oracle's
-C restatement of SQUANDER's BFGS decomposition; the reference itself is not buildable
-here).
+C restatement of SQUANDER's BFGS decomposition; the reference itself needs TBB and
+CBLAS, which are not installed, so it is not built).
 """
 import argparse
 import importlib
@@ -585,7 +585,7 @@ def bench_decompose_n6(sqg, wl, torch):
 
 
 def bench_cost_grad_n10(sqg, wl, torch):
-    """BASELINE config 3 shape: n = 10, 300 CNOT blocks over uniformly drawn ordered pairs
+    """The n = 10 workload: 300 CNOT blocks over uniformly drawn ordered pairs
     (P = 1830), cost + adjoint gradient of 64 parameter vectors, plain and checkpointed."""
     rng = np.random.default_rng(12)
     c = wl.cnot_u3_ansatz(10, 300, pairs="random", rng=rng)

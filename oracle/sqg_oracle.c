@@ -9,7 +9,7 @@
  * It is the checker for the CUDA engine (tests, smoke(), the CPU-baseline leg of
  * bench.py).  Nothing in the engine links or calls it.  Every routine follows the
  * reference algorithm step by step, including its summation order and its
- * "(1 - tr/N) - 1" gradient formula, so that parity can be judged against the
+ * "(1 - tr/N) - 1" gradient formula, so that parity can be checked against the
  * reference's own arithmetic.  Reference citations are paths inside the
  * SQUANDER tree (src-cpp = squander/src-cpp).
  *

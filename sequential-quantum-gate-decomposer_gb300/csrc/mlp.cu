@@ -1,8 +1,8 @@
 // Kernels of the learned initialiser (an MLP mapping a target unitary to starting angles):
 // BF16 GEMM with FP32 accumulation on the tensor cores, fused bias/ReLU epilogues, the
 // backward-pass helpers, the angle head and Adam.  The initialiser has no counterpart in
-// SQUANDER; it only proposes start points for the decomposition kernels, which remain the
-// judge of every result.
+// SQUANDER; it only proposes start points for the decomposition kernels, whose FP64 cost
+// decides every result.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 

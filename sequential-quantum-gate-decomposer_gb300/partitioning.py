@@ -205,7 +205,7 @@ def PartitionCircuit(circ, parameters, max_partition_size, strategy="kahn", file
     (partitioned circuit, its parameters, partitions).  Unknown strategy names use "kahn", as
     in the reference."""
     if strategy in _UNAVAILABLE:
-        raise NotImplementedError("partitioning strategy %r needs %s, which this build does not include; use "
+        raise NotImplementedError("partitioning strategy %r needs %s, which this package does not include; use "
                                   "'kahn'" % (strategy, _UNAVAILABLE[strategy]))
     if strategy in ("tdag", "gtqcp"):
         raise NotImplementedError("partitioning strategy %r is not restated; use 'kahn'" % strategy)

@@ -1,6 +1,6 @@
 """What the trained initialiser gains over the plain random start (the method without it):
 trained on the GPU with the engine's own kernels on decompositions the method generates,
-evaluated on held-out targets by the FP64 decomposition kernel, which stays the judge."""
+evaluated on held-out targets by the FP64 decomposition kernel, whose cost decides each result."""
 import importlib
 
 import numpy as np
