@@ -163,6 +163,11 @@ def bfgs_flops_per_iteration(P):
     return 17 * P * P
 
 
+# DRAM bytes of one k_decompose launch of the timed workload (4096 targets), measured once with
+# ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (one pass, --profile-case decompose_full)
+K_DECOMPOSE_DRAM_BYTES = 6.06e9 + 56.85e9
+
+
 def bench_learned(sqg, wl, torch, ansatz, targets, tdev, plain_rate, plain_solved, steps):
     """Learned path: the MLP initialiser (trained here on GPU-generated decompositions of
     204800 synthetic targets, supervised, tcgen05 GEMMs) proposes the start points; each
@@ -288,7 +293,10 @@ def bench_ours(args):
         "gpu_launches": args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
                      "peak_source": "measured live by the FP64 probe kernel",
-                     "frac": achieved_tflops / FP64_PEAK_TFLOPS, "traffic": None,
+                     "frac": achieved_tflops / FP64_PEAK_TFLOPS, "traffic": K_DECOMPOSE_DRAM_BYTES,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_decompose launch of "
+                                       "this workload (ncu, one pass): 6.06 GB read, 56.85 GB written, mostly the "
+                                       "per-target BFGS matrices Z (69 KB each) written back from L2",
                      "note": "k_decompose is FP64-issue bound (HBM idle); achieved = algorithmic flops of the "
                              "evaluations (3 passes x 16 flop per complex element per parametric gate) and BFGS "
                              "iterations (17 P^2) performed, over the timed steps",
@@ -740,6 +748,15 @@ def profile_case(case, profile_calls=60):
         dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=profile_calls, max_outer=1,
                                     stop_at_tolerance=profile_calls == 60)
         x, cost, calls = dec.run(torch.from_numpy(targets[:B]).cuda(), rng.uniform(0, 2 * np.pi, (B, P)))
+    elif case == "decompose_full":
+        # one launch of the timed step itself: all 4096 targets, the bench's budgets (for the
+        # one-pass DRAM byte counters only)
+        ansatz, targets = make_workload(sqg, wl)
+        P = ansatz.get_Parameter_Num()
+        dec = sqg.BatchedDecomposer(ansatz, tolerance=TOL, max_calls=MAX_CALLS, max_outer=MAX_OUTER)
+        x, cost, calls = dec.run(torch.from_numpy(targets).cuda(), rng.uniform(0, 2 * np.pi, (N_TARGETS, P)), seed=1000)
+        torch.cuda.synchronize()
+        print(json.dumps({"evaluations": int(calls.sum().item()), "bfgs_iterations": int(dec.iters.sum().item())}))
     elif case == "gate_apply":
         c = wl.random_gate_circuit(12, 200, rng)
         th = torch.from_numpy(rng.uniform(0, 2 * np.pi, (1, c.get_Parameter_Num()))).cuda()
@@ -808,7 +825,7 @@ def profile_case(case, profile_calls=60):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe-fp64", action="store_true", help="print the live FP64 FMA peak by active lanes")
-    ap.add_argument("--profile-case", choices=["decompose", "gate_apply", "cost_grad", "mlp_gemm", "dropin_bfgs_n6",
+    ap.add_argument("--profile-case", choices=["decompose", "decompose_full", "gate_apply", "cost_grad", "mlp_gemm", "dropin_bfgs_n6",
                                                      "state_vector", "env_costgrad", "ragged"],
                     default=None)
     ap.add_argument("--profile-calls", type=int, default=60,
