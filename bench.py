@@ -297,7 +297,7 @@ def bench_ours(args):
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_decompose launch of "
                                        "this workload (ncu, one pass): 6.06 GB read, 56.85 GB written, mostly the "
                                        "per-target BFGS matrices Z (69 KB each) written back from L2",
-                     "note": "k_decompose is FP64-issue bound (HBM idle); achieved = algorithmic flops of the "
+                     "note": "k_decompose is FP64-issue bound (HBM at 1.7%); achieved = algorithmic flops of the "
                              "evaluations (3 passes x 16 flop per complex element per parametric gate) and BFGS "
                              "iterations (17 P^2) performed, over the timed steps",
                      "flops_per_eval": flops_eval, "flops_per_bfgs_iteration": bfgs_flops_per_iteration(P)},
