@@ -118,6 +118,54 @@ def test_six_qubit_first_bfgs_steps_follow_the_oracle(sqg, wl, monkeypatch, cols
     assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)
 
 
+@pytest.mark.parametrize("variant", [O.FROBENIUS_NORM, O.HILBERT_SCHMIDT_TEST, O.INFIDELITY])
+def test_six_qubit_mixed_gates_follow_the_oracle(sqg, wl, variant):
+    """Six qubits with every gate kind the engine takes (U3, RY, CNOT, CZ, CRY drawn at random,
+    then RX and RZ on every qubit) and all three cost variants: the first BFGS steps match the
+    oracle's."""
+    n = 6
+    rng = np.random.default_rng(90 + variant)
+    c = wl.random_gate_circuit(n, 40, rng)
+    for q in range(n):
+        c.add_RX(q)
+        c.add_RZ(q)
+    P = c.get_Parameter_Num()
+    recs = c.gate_records()
+    B = 3
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, recs, rng.uniform(0, 2 * np.pi, P)).conj().T)
+                        for _ in range(B)])
+    x0 = rng.uniform(0, 2 * np.pi, (B, P))
+    dec = sqg.BatchedDecomposer(c, tolerance=0.0, max_calls=5, max_outer=1, stop_at_tolerance=False,
+                                cost_variant=variant)
+    x, cost, calls = dec.run(targets, x0)
+    torch.cuda.synchronize()
+    xr, cr, callr = O.decompose(n, recs, targets, x0, tolerance=0.0, max_inner=5, max_outer=1, variant=variant)
+    assert np.array_equal(calls.cpu().numpy(), callr)
+    assert np.allclose(cost.cpu().numpy(), cr, rtol=1e-9, atol=1e-12)
+    assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)
+
+
+def test_six_qubit_adam_follows_the_oracle(sqg, wl):
+    """Six-qubit targets with SQUANDER's ADAM engine per CTA (four warps, target read from L2)
+    against the oracle's restatement: the same evaluation counts and trajectory to rounding."""
+    n = 6
+    rng = np.random.default_rng(95)
+    c = wl.cnot_u3_ansatz(n, 2)
+    P = c.get_Parameter_Num()
+    targets = np.stack([np.ascontiguousarray(O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, P)).conj().T)
+                        for _ in range(3)])
+    x0 = rng.uniform(0, 2 * np.pi, (3, P))
+    dec = sqg.BatchedDecomposer(c, tolerance=1e-8, max_calls=60, max_outer=1, optimizer="ADAM", eta=1e-3)
+    x, cost, evals = dec.run(targets, x0, seed=5)
+    torch.cuda.synchronize()
+    xr, cr, er, sr = O.adam_decompose(n, c.gate_records(), targets, x0, tolerance=1e-8, max_iters=60, eta=1e-3,
+                                      adaptive_eta=True, seed=5)
+    assert np.array_equal(evals.cpu().numpy(), er)
+    assert np.array_equal(dec.iters.cpu().numpy(), sr)
+    assert np.allclose(cost.cpu().numpy(), cr, rtol=1e-9, atol=1e-12)
+    assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)
+
+
 def test_six_qubit_exact_start_and_restart(sqg, wl):
     """Six-qubit targets built by the circuit: an exact start stops after one evaluation, a
     perturbed one converges below the tolerance (checked by the oracle's cost)."""
