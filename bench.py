@@ -706,18 +706,21 @@ def bench_reference(args):
     recs = ansatz.gate_records()
     threads = os.cpu_count() or 1
     rng = np.random.default_rng(77)
-    per_step = max(threads, int(args.ref_targets))
+    # 16 targets per host thread and step: the work queue then balances the long-running
+    # decompositions (up to 4000 evaluations) against the short ones, as the GPU's batch does
+    per_step = int(args.ref_targets) if args.ref_targets > 0 else 16 * threads
+    per_step = max(threads, per_step)
 
-    def step(k):
-        idx = (np.arange(per_step) + k * per_step) % N_TARGETS
-        x0 = rng.uniform(0, 2 * np.pi, (per_step, P))
+    def step(k, count=per_step):
+        idx = (np.arange(count) + k * per_step) % N_TARGETS
+        x0 = rng.uniform(0, 2 * np.pi, (count, P))
         t0 = time.perf_counter()
         _, cost, _ = orc.decompose(3, recs, targets[idx], x0, tolerance=TOL, max_inner=MAX_CALLS,
                                    max_outer=MAX_OUTER, nthreads=threads, seed=k)
         return time.perf_counter() - t0, int((cost < TOL).sum())
 
-    for w in range(args.warmup):
-        step(100 + w) if per_step <= 64 else None
+    for w in range(args.warmup):  # one target per thread: warms the library and the threads
+        step(100 + w, count=threads)
     times, solved = [], 0
     for k in range(args.steps):
         t, s = step(k)
@@ -838,7 +841,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-learned", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--ref-targets", type=int, default=32)
+    ap.add_argument("--ref-targets", type=int, default=0, help="targets per reference step (0: 16 per host thread)")
     args = ap.parse_args()
     if args.probe_fp64:
         native = importlib.import_module(PKG + "._native")
