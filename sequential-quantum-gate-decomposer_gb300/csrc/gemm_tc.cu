@@ -3,14 +3,14 @@
 // initialiser's layer GEMMs.  C[M][N] = A[M][K] * B[N][K]^T (+ bias[n], optional ReLU),
 // both operands K-major bf16, FP32 accumulation; results as fp32 and/or bf16.
 //
-// One CTA computes a 128 x 128 tile: warp 0 allocates 128 TMEM columns; one thread of warp
-// 0 issues the TMA loads into a ring of four stages (128 x 64 of A and of B each) and waits
-// only for a stage's "empty" barrier, one thread of warp 1 issues the MMAs (4 x K=16 per
-// stage) and commits each stage to that barrier; finally the four warps read their 32 TMEM
-// lanes each (32x32b loads) into a padded shared-memory tile and store it row by row
-// (coalesced), with the bias / ReLU epilogue.  Every mbarrier wait is bounded: on a
-// time-out the CTA records an error code, drains its own copies and MMAs (again bounded),
-// frees its TMEM and returns.
+// One CTA computes a 128 x TN tile (TN = 256 where N is a multiple of 256, else 128): warp 0
+// allocates TN TMEM columns; one thread of warp 0 issues the TMA loads into a ring of four
+// stages (128 x 64 of A, TN x 64 of B) and waits only for a stage's "empty" barrier, one
+// thread of warp 1 issues the MMAs (4 x 128 x TN x 16 per stage) and commits each stage to
+// that barrier; finally the four warps read their 32 TMEM lanes each (32x32b loads) into a
+// padded shared-memory tile and store it row by row (coalesced), with the bias / ReLU
+// epilogue.  Every mbarrier wait is bounded: on a time-out the CTA records an error code,
+// drains its own copies and MMAs (again bounded), frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -23,10 +23,8 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 64, STAGES = 4;
-constexpr int STAGE_BYTES = (TM + TN) * TK * 2;  // 32 KB
-constexpr int EPI_LD = TN + 1;                   // fp32 epilogue tile row (odd: no bank conflicts)
-static_assert(TM * EPI_LD * 4 <= STAGES * STAGE_BYTES, "the epilogue tile reuses the stage buffers");
+constexpr int TM = 128, TK = 64;
+__host__ __device__ constexpr int stage_bytes(int TN) { return (TM + TN) * TK * 2; }
 constexpr unsigned kSpinLimit = 1u << 24;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -39,12 +37,14 @@ __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
 __device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
-// Bounded wait for the phase with the given parity; returns false on time-out.
+// Bounded wait for the phase with the given parity; returns false on time-out.  Polls with the
+// non-blocking test_wait: try_wait may suspend the thread for a hardware-chosen interval, which
+// a producer or MMA thread that arrives just before the phase completes would pay every k-step.
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
   for (unsigned i = 0; i < kSpinLimit; i++) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
         : "r"(bar), "r"(parity)
         : "memory");
@@ -77,10 +77,14 @@ __host__ __device__ constexpr unsigned instr_desc(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
 }
 
+template <int TN, int STAGES>
 __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUtensorMap mapA,
                                                      const __grid_constant__ CUtensorMap mapB, int M, int N, int K,
                                                      float* __restrict__ C, int ldc, const float* __restrict__ bias,
                                                      int relu, __nv_bfloat16* __restrict__ Cb, int* err) {
+  constexpr int STAGE_BYTES = stage_bytes(TN);
+  constexpr int EPI_LD = TN + 1;  // fp32 epilogue tile row (odd: no bank conflicts)
+  static_assert(TM * EPI_LD * 4 <= STAGES * STAGE_BYTES, "the epilogue tile reuses the stage buffers");
   extern __shared__ __align__(1024) unsigned char dsmem[];
   // 1024-byte alignment for the swizzled tiles
   unsigned char* base = (unsigned char*)(((unsigned long long)dsmem + 1023) & ~1023ull);
@@ -103,7 +107,8 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&tmem_base_s)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(TN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -210,7 +215,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TN));
 }
 
 // bf16 transpose: out[c][r] = in[r][c] (rows x cols, row strides in elements).
@@ -246,19 +251,40 @@ EncodeTiled encode_fn() {
   return fn;
 }
 
-// 2-D K-major bf16 tensor map: rows x K elements, row stride ld elements, box 64 x 128.
-int make_map(CUtensorMap* map, const void* ptr, int rows, int K, int ld) {
+// 2-D K-major bf16 tensor map: rows x K elements, row stride ld elements, box 64 x box_rows.
+int make_map(CUtensorMap* map, const void* ptr, int rows, int K, int ld, int box_rows) {
   EncodeTiled enc = encode_fn();
   if (!enc) return sqg::set_error(SQG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  cuuint32_t box[2] = {TK, 128};
+  cuuint32_t box[2] = {TK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return sqg::set_error(SQG_ERR_INVALID_ARGUMENT, "cuTensorMapEncodeTiled failed");
   return SQG_OK;
+}
+
+template <int TN, int STAGES>
+int gemm_launch(int M, int N, int K, const void* A, int lda, const void* B, int ldb, float* C, int ldc,
+                const float* bias, int relu, void* C_bf16, int* err_dev, void* stream) {
+  CUtensorMap ma, mb;
+  int st;
+  if ((st = make_map(&ma, A, M, K, lda, TM))) return st;
+  if ((st = make_map(&mb, B, N, K, ldb, TN))) return st;
+  const size_t smem = (size_t)STAGES * stage_bytes(TN) + 1024;
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [&]() {
+    attr = cudaFuncSetAttribute(k_gemm_tc<TN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  if (attr != cudaSuccess) return sqg::set_error(SQG_ERR_CUDA, cudaGetErrorString(attr));
+  dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
+  k_gemm_tc<TN, STAGES><<<grid, 128, smem, (cudaStream_t)stream>>>(ma, mb, M, N, K, C, ldc, bias, relu,
+                                                                   (__nv_bfloat16*)C_bf16, err_dev);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SQG_OK : sqg::set_error(SQG_ERR_CUDA, std::string("k_gemm_tc: ") + cudaGetErrorString(e));
 }
 
 }  // namespace
@@ -272,22 +298,10 @@ int sqg_mlp_gemm_tc(int M, int N, int K, const void* A, int lda, const void* B, 
   if (K % 8 || lda % 8 || ldb % 8 || ((unsigned long long)A & 15) || ((unsigned long long)B & 15))
     return sqg::set_error(SQG_ERR_INVALID_ARGUMENT,
                           "tensor-core GEMM needs 16-byte aligned operands and K, lda, ldb multiples of 8");
-  CUtensorMap ma, mb;
-  int st;
-  if ((st = make_map(&ma, A, M, K, lda))) return st;
-  if ((st = make_map(&mb, B, N, K, ldb))) return st;
-  const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [&]() {
-    attr = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  });
-  if (attr != cudaSuccess) return sqg::set_error(SQG_ERR_CUDA, cudaGetErrorString(attr));
-  dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
-  k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>(ma, mb, M, N, K, C, ldc, bias, relu, (__nv_bfloat16*)C_bf16,
-                                                       err_dev);
-  cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? SQG_OK : sqg::set_error(SQG_ERR_CUDA, std::string("k_gemm_tc: ") + cudaGetErrorString(e));
+  // 128 x 256 tiles (one 128 x 256 x 16 MMA per K = 16 step, B read once per 256 columns) where
+  // N fills them; 128 x 128 for narrow or ragged N, where a 256-wide tile would idle columns
+  if (N % 256 == 0) return gemm_launch<256, 4>(M, N, K, A, lda, B, ldb, C, ldc, bias, relu, C_bf16, err_dev, stream);
+  return gemm_launch<128, 4>(M, N, K, A, lda, B, ldb, C, ldc, bias, relu, C_bf16, err_dev, stream);
 }
 
 int sqg_mlp_transpose_bf16(const void* in, int rows, int cols, int ld_in, void* out, int ld_out, void* stream) {
