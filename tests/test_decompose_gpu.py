@@ -259,3 +259,71 @@ def test_device_adam_follows_the_oracle(sqg, wl, case):
     else:
         assert np.allclose(cost.cpu().numpy(), cr, rtol=1e-9, atol=1e-12)
         assert np.allclose(x.cpu().numpy(), xr, atol=1e-8)
+
+
+def test_batched_argument_errors(sqg, wl):
+    """The batched entry points reject bad arguments with a status before launching, as the
+    reference's wrapper raises on bad input (qgd_N_Qubit_Decompositions_Wrapper.cpp:1404-1432)."""
+    native = importlib.import_module("sequential-quantum-gate-decomposer_gb300._native")
+    n = 3
+    rng = np.random.default_rng(97)
+    c = wl.cnot_u3_ansatz(n, 2)
+    P = c.get_Parameter_Num()
+    T = np.ascontiguousarray(O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, P)).conj().T)[None]
+    x0 = rng.uniform(0, 2 * np.pi, (1, P))
+    with pytest.raises(native.SQGError, match="unsupported configuration"):
+        sqg.BatchedDecomposer(c, cost_variant=5).run(T, x0)
+    with pytest.raises(native.SQGError, match="trace offset out of range"):
+        sqg.BatchedDecomposer(c, trace_offset=2).run(T[:, :, :7], x0)
+    with pytest.raises(native.SQGError, match="iteration limits"):
+        sqg.BatchedDecomposer(c, max_calls=0).run(T, x0)
+    with pytest.raises(native.SQGError, match="iteration limits"):
+        sqg.BatchedDecomposer(c, optimizer="ADAM", max_outer=0).run(T, x0)
+    with pytest.raises(ValueError):
+        sqg.BatchedDecomposer(c).run(T, x0[:, :-1])
+    torch.cuda.synchronize()
+
+
+def test_structure_batch_argument_errors(sqg, wl):
+    """sqg_decompose_structures checks every gate list against the circuit's gate types and
+    parameter layout and every qubit index before it copies anything, and its workspace size
+    and alignment."""
+    native = importlib.import_module("sequential-quantum-gate-decomposer_gb300._native")
+    ts = importlib.import_module("sequential-quantum-gate-decomposer_gb300.tree_search")
+    dev = importlib.import_module("sequential-quantum-gate-decomposer_gb300._device")
+    n = 3
+    topo = ts.normalize_topology(None, n)
+    codes = ts.level_codes(2, topo)[:4]
+    circ = ts.structure_circuit(codes[0], topo, n)
+    nc = circ.native()
+    P, B = nc.param_num, codes.shape[0]
+    recs = np.ascontiguousarray(ts.structure_records(codes, topo, n))
+    lib = native.lib()
+    target = torch.as_tensor(np.ascontiguousarray(np.eye(8, dtype=np.complex128)), device="cuda")
+    x = torch.zeros((B, P), dtype=torch.float64, device="cuda")
+    cost = torch.empty(B, dtype=torch.float64, device="cuda")
+    calls = torch.empty(B, dtype=torch.int32, device="cuda")
+    need = lib.sqg_decompose_structures_workspace_bytes(nc.handle, B, 8)
+    w = dev.Workspace().get(need)
+
+    def call(records, ws_ptr, ws_bytes):
+        return lib.sqg_decompose_structures(nc.handle, records.ctypes.data, dev.ptr(target), 0, 8, B, 0, 0,
+                                            dev.ptr(x), dev.ptr(cost), dev.ptr(calls), None, 1e-8, 5, 1, 1, 0, 1,
+                                            ws_ptr, ws_bytes, None)
+
+    assert call(recs, dev.ptr(w), w.numel()) == 0
+    torch.cuda.synchronize()
+    # records: (B, gates, 4) int32 of (type, target, control, parameter start)
+    cnot = int(np.nonzero(recs[1, :, 2] >= 0)[0][0])
+    bad = recs.copy()
+    bad[1, cnot, 0] = recs[1, 0, 0]  # a controlled gate of list 1 turned into the first gate's kind
+    assert call(bad, dev.ptr(w), w.numel()) == 1
+    bad = recs.copy()
+    bad[-1, -1, 1] = n  # qubit out of range
+    assert call(bad, dev.ptr(w), w.numel()) == 1
+    bad = recs.copy()
+    bad[2, cnot, 2] = bad[2, cnot, 1]  # control equal to the target
+    assert call(bad, dev.ptr(w), w.numel()) == 1
+    assert call(recs, dev.ptr(w), need - 256) == 3  # workspace too small
+    assert call(recs, dev.ptr(w) + 8, w.numel() - 8) == 3  # not 256-byte aligned
+    torch.cuda.synchronize()
