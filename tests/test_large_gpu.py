@@ -51,6 +51,44 @@ def test_n10_adjoint_gradient_finite_differences_and_checkpoints(sqg, wl):
     assert c0.item() > 1e-3
 
 
+def test_n10_adam_then_bfgs_with_and_without_checkpoints(sqg, wl):
+    """n = 10 decomposition in two phases: torch.optim.Adam through the differentiable cost
+    (the adjoint kernel behind torch.autograd.Function), once with the plain adjoint gradient
+    and once with checkpointed partial products every 8 gates, then the device BFGS loop to
+    cost < 1e-8.  The two Adam trajectories agree to rounding; the final cost is certified by a
+    fresh evaluation."""
+    batched = importlib.import_module("sequential-quantum-gate-decomposer_gb300.batched")
+    rng = np.random.default_rng(23)
+    c = wl.cnot_u3_ansatz(10, 12, pairs="random", rng=rng)
+    P = c.get_Parameter_Num()
+    p = rng.uniform(0, 2 * np.pi, P)
+    T = np.ascontiguousarray(c.get_Matrix(p).conj().T)
+    ev = sqg.CostEvaluator(c, T)
+    start = p + rng.normal(0.0, 0.05, P)
+    ends = []
+    for interval in (0, 8):
+        theta = torch.tensor(start, device="cuda", requires_grad=True)
+        opt = torch.optim.Adam([theta], lr=2e-3)
+        f0 = None
+        for _ in range(100):
+            opt.zero_grad()
+            f = sqg.circuit_cost(theta, ev, checkpoint_interval=interval)
+            f0 = f.item() if f0 is None else f0
+            f.sum().backward()
+            opt.step()
+        ends.append((theta.detach().clone(), f.item(), f0))
+    (xa, fa, f0a), (xb, fb, f0b) = ends
+    assert f0a == pytest.approx(f0b, rel=1e-12)
+    assert fa < 0.5 * f0a
+    assert float((xa - xb).abs().max()) < 1e-9
+    x, cost, calls, _ = batched.bfgs_decompose_graph(c, T, xa, tolerance=1e-8, max_calls=3000, max_outer=1)
+    torch.cuda.synchronize()
+    assert cost.item() < 1e-8
+    check, _ = ev.cost_grad(x.reshape(1, -1), with_grad=False)
+    assert check.item() < 1e-8
+    assert 0 < int(calls.item()) <= 3000
+
+
 def test_n10_exact_solution(sqg, wl):
     rng = np.random.default_rng(22)
     c = wl.cnot_u3_ansatz(10, 60, pairs="random", rng=rng)
