@@ -670,8 +670,9 @@ def cpu_baseline(sqg, wl, ansatz, targets, P, budget_s=20.0):
     threads = os.cpu_count() or 1
     recs = ansatz.gate_records()
     rng = np.random.default_rng(77)
-    # bounded sample: grow the number of targets until about budget_s of CPU work
-    n = threads
+    # bounded sample: calls of 16 targets per host thread (the work queue balances the long
+    # decompositions against the short ones) until about budget_s of CPU work
+    n = 16 * threads
     t0 = time.perf_counter()
     solved, done = 0, 0
     while True:
@@ -760,6 +761,14 @@ def profile_case(case, profile_calls=60):
         x, cost, calls = dec.run(torch.from_numpy(targets).cuda(), rng.uniform(0, 2 * np.pi, (N_TARGETS, P)), seed=1000)
         torch.cuda.synchronize()
         print(json.dumps({"evaluations": int(calls.sum().item()), "bfgs_iterations": int(dec.iters.sum().item())}))
+    elif case == "decompose_n6":
+        # six-qubit targets, one CTA each (608 targets, at most 60 evaluations, one run)
+        c = wl.cnot_u3_ansatz(6, 3)
+        P = c.get_Parameter_Num()
+        T = np.stack([np.ascontiguousarray(c.get_Matrix(rng.uniform(0, 2 * np.pi, P)).conj().T) for _ in range(608)])
+        dec = sqg.BatchedDecomposer(c, tolerance=TOL, max_calls=profile_calls, max_outer=1)
+        x, cost, calls = dec.run(torch.from_numpy(T).cuda(), rng.uniform(0, 2 * np.pi, (608, P)))
+        torch.cuda.synchronize()
     elif case == "gate_apply":
         c = wl.random_gate_circuit(12, 200, rng)
         th = torch.from_numpy(rng.uniform(0, 2 * np.pi, (1, c.get_Parameter_Num()))).cuda()
@@ -828,7 +837,7 @@ def profile_case(case, profile_calls=60):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe-fp64", action="store_true", help="print the live FP64 FMA peak by active lanes")
-    ap.add_argument("--profile-case", choices=["decompose", "decompose_full", "gate_apply", "cost_grad", "mlp_gemm", "dropin_bfgs_n6",
+    ap.add_argument("--profile-case", choices=["decompose", "decompose_full", "decompose_n6", "gate_apply", "cost_grad", "mlp_gemm", "dropin_bfgs_n6",
                                                      "state_vector", "env_costgrad", "ragged"],
                     default=None)
     ap.add_argument("--profile-calls", type=int, default=60,
