@@ -697,7 +697,6 @@ def bench_reference(args):
 
     sqg = importlib.import_module(PKG)
     wl = importlib.import_module(PKG + ".workloads")
-    ansatz_rec = None
 
     def mat(circ, theta):
         return orc.get_matrix(circ.qbit_num, circ.gate_records(), theta)

@@ -6,8 +6,6 @@
 B parameter vectors are evaluated against one shared target U^dagger or one target per
 instance in a single launch of the column-tile kernels (sqg_cost_grad).
 """
-import numpy as np
-
 from . import _device as dev
 from . import _native
 from .circuit import Circuit, NativeCircuit

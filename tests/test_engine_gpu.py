@@ -141,6 +141,7 @@ def test_checkpointed_gradient_equals_uncomputed(sqg):
     assert_close(c1.cpu().numpy(), c0.cpu().numpy())
     assert_close(g1.cpu().numpy(), g0.cpu().numpy())
     rc, rg = O.batch(n, c.gate_records(), theta.cpu().numpy(), target, with_grad=True)
+    assert_close(c1.cpu().numpy(), rc)
     assert_close(g1.cpu().numpy(), rg)
 
 

@@ -46,8 +46,8 @@ def test_n10_adjoint_gradient_finite_differences_and_checkpoints(sqg, wl):
     # checkpointed partial products give the same gradient
     c2, g2 = ev.cost_grad(theta.detach()[:2], checkpoint_interval=30)
     assert float((g2 - g[:2]).abs().max()) <= 1e-12 * max(1.0, float(g[:2].abs().max()))
-    # at the exact parameters the cost and the gradient vanish
-    c0, g0 = ev.cost_grad(torch.from_numpy(np.asarray(rng.uniform(0, 1, P))).cuda())
+    # away from the solution the cost does not vanish
+    c0, _ = ev.cost_grad(torch.from_numpy(np.asarray(rng.uniform(0, 1, P))).cuda())
     assert c0.item() > 1e-3
 
 
@@ -79,7 +79,7 @@ def test_n10_adam_then_bfgs_with_and_without_checkpoints(sqg, wl):
         ends.append((theta.detach().clone(), f.item(), f0))
     (xa, fa, f0a), (xb, fb, f0b) = ends
     assert f0a == pytest.approx(f0b, rel=1e-12)
-    assert fa < 0.5 * f0a
+    assert fa < 0.5 * f0a and fb == pytest.approx(fa, rel=1e-9)
     assert float((xa - xb).abs().max()) < 1e-9
     x, cost, calls, _ = batched.bfgs_decompose_graph(c, T, xa, tolerance=1e-8, max_calls=3000, max_outer=1)
     torch.cuda.synchronize()

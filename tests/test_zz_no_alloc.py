@@ -3,7 +3,6 @@ device memory (for instance a cost callback behind an optimizer interface that p
 the parameters, the cost and the gradient).  It runs the same kernels as sqg_cost_grad on a
 32 MiB scratch array built into the library.  This file is collected last so that a run
 stopping at the first failure has run every other test first."""
-import ctypes
 import importlib
 
 import numpy as np
