@@ -724,15 +724,35 @@ size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem, bool adam 
 
 constexpr size_t kDecSmemLimit = 110 * 1024;  // keep two CTAs per SM
 
-// Per-instance BFGS matrices stay in shared memory only while they are small (<= 16 KB):
-// beyond that, keeping them in the caller's workspace (L2-resident for the ~1000
-// instances in flight) lets several times more instances share an SM, and the kernel
-// is bound by FP64 issue, not by L2.  SQG_DECOMPOSE_Z=global|shared overrides the rule.
+// Decomposition CTAs one SM holds with `threads` threads and `smem` bytes of dynamic shared
+// memory each: the smaller of the shared-memory and the register limit (80 registers a thread,
+// as __launch_bounds__ fixes them).
+int dec_ctas_per_sm(int threads, size_t smem) {
+  static int per_sm = -1, reserved = 1024;
+  if (per_sm < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    per_sm = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess ? v
+                                                                                                       : 228 * 1024;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess) reserved = v;
+  }
+  const size_t by_smem = (size_t)per_sm / (smem + (size_t)reserved);
+  const size_t by_regs = 65536 / (80 * (size_t)threads);
+  return (int)std::min(by_smem, by_regs);
+}
+
+// Per-instance BFGS matrices stay in shared memory only while they are small (<= 16 KB) and
+// cost no resident CTA: beyond that, keeping them in the caller's workspace (L2-resident for
+// the instances in flight) lets more instances share an SM, and the kernel is bound by FP64
+// issue, not by L2 (six qubits, P = 36: 3 CTAs per SM instead of 2, +8.7%).
+// SQG_DECOMPOSE_Z=global|shared overrides the rule.
 bool z_in_shared(const sqg_circuit* c, int cols) {
   const char* zenv = getenv("SQG_DECOMPOSE_Z");
   if (zenv && std::string(zenv) == "global") return false;
   if (zenv && std::string(zenv) == "shared") return dec_smem_bytes(c, cols, true) <= 227 * 1024;
-  return (size_t)c->P * c->P * sizeof(double) <= 16 * 1024 && dec_smem_bytes(c, cols, true) <= kDecSmemLimit;
+  const size_t with_z = dec_smem_bytes(c, cols, true);
+  return (size_t)c->P * c->P * sizeof(double) <= 16 * 1024 && with_z <= kDecSmemLimit &&
+         dec_ctas_per_sm(dec_threads(c), with_z) >= dec_ctas_per_sm(dec_threads(c), dec_smem_bytes(c, cols, false));
 }
 
 // The environment-matrix form costs 3 N^2 / 2 amplitude-pair updates per gate against
