@@ -242,9 +242,16 @@ __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* 
   dec_build(a, sh, xv);
   double2* m = sh.psi;  // N * N entries: psi alone when cols = N, else psi and the contiguous lam
   const double2* T = sh.tgt;
-  for (int e = threadIdx.x; e < NN; e += blockDim.x) {
-    const int c = e >> n, r = e & (N - 1), j = c - off;
-    m[e] = (j >= 0 && j < cols) ? T[r * cols + j] : make_double2(0.0, 0.0);
+  // M_0[r][j + off] = T[r][j] (m column-major), zero outside the target's columns; walked in
+  // the target's row-major order so that a target read from L2 is read coalesced
+  if (cols != N || off != 0)
+    for (int e = threadIdx.x; e < NN; e += blockDim.x) {
+      const int j = (e >> n) - off;
+      if (j < 0 || j >= cols) m[e] = make_double2(0.0, 0.0);
+    }
+  for (int e = threadIdx.x; e < N * cols; e += blockDim.x) {
+    const int r = e / cols, j = e - r * cols;
+    m[(j + off) * N + r] = T[e];
   }
   __syncthreads();
   const int aw = min((int)(blockDim.x >> 5), (NN / 2 + 31) >> 5);
@@ -695,11 +702,6 @@ bool dec_needs_lam(const sqg_circuit* c, int cols) {
   return c->N * c->N / 2 <= 32 && c->L >= 2 && use_two_chains();
 }
 
-// Six-qubit targets (up to 64 KB) stay in global memory: a copy in shared memory would halve the
-// CTAs an SM holds, and the evaluation reads the target once (into the environment matrix or
-// the first state), from L2.
-bool dec_target_in_smem(const sqg_circuit* c) { return c->n <= 5; }
-
 // Threads of a decomposition CTA: one per parameter for the vector and Z-matrix work, at least
 // two warps; four at six qubits, where shared memory admits few CTAs per SM and the
 // evaluation's 2048 amplitude pairs per gate keep every warp busy.
@@ -708,21 +710,21 @@ int dec_threads(const sqg_circuit* c) {
   return std::min(kDecThreads, std::max(64, (c->P + 31) / 32 * 32));
 }
 
-size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem, bool adam = false) {
+// Shared memory of one decomposition CTA with the target (tgt) and the BFGS matrix Z (z) on
+// chip or not; adam: the ADAM engine's extra windows instead of Z.
+size_t dec_smem_layout(const sqg_circuit* c, int cols, bool tgt, bool z, bool adam) {
   auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t P = std::max(c->P, 1), L = std::max(c->L, 1), NC = (size_t)c->N * cols;
   // psi, lambda unless the form needs none, the target unless it stays in global memory
-  const size_t tiles = 1 + (dec_needs_lam(c, cols) ? 1 : 0) + (dec_target_in_smem(c) ? 1 : 0);
+  const size_t tiles = 1 + (dec_needs_lam(c, cols) ? 1 : 0) + (tgt ? 1 : 0);
   size_t s = r16(sizeof(Gate) * L) + tiles * r16(sizeof(double2) * NC) + r16(sizeof(GateMat) * L) + r16(sizeof(double2) * P) +
              r16(sizeof(double) * 8 * L) + r16(sizeof(int) * P) + r16(sizeof(int) * L) +
              kDecVectors * r16(sizeof(double) * P) + r16(sizeof(double) * kTileMaxWarps * 8) + r16(sizeof(double) * 8) +
              r16(sizeof(double) * kTileMaxWarps);
   if (adam) return s + r16(sizeof(double) * 100) + r16(sizeof(int) * 20);
-  if (z_in_smem) s += r16(sizeof(double) * P * P);
+  if (z) s += r16(sizeof(double) * P * P);
   return s;
 }
-
-constexpr size_t kDecSmemLimit = 110 * 1024;  // keep two CTAs per SM
 
 // Decomposition CTAs one SM holds with `threads` threads and `smem` bytes of dynamic shared
 // memory each: the smaller of the shared-memory and the register limit (80 registers a thread,
@@ -740,6 +742,27 @@ int dec_ctas_per_sm(int threads, size_t smem) {
   const size_t by_regs = 65536 / (80 * (size_t)threads);
   return (int)std::min(by_smem, by_regs);
 }
+
+// The target stays in shared memory only if that costs no resident CTA (decided with Z off
+// chip): the evaluation reads it once (into the environment matrix or the first state), so
+// from L2 it costs one coalesced read per evaluation, while a shared copy of a six-qubit
+// target (64 KB) would halve the CTAs an SM holds.  SQG_DECOMPOSE_TARGET=global|shared
+// overrides the rule below six qubits.
+bool dec_target_in_smem(const sqg_circuit* c, int cols) {
+  if (c->n >= 6) return false;
+  const char* tenv = getenv("SQG_DECOMPOSE_TARGET");
+  if (tenv && std::string(tenv) == "global") return false;
+  if (tenv && std::string(tenv) == "shared") return true;
+  const int t = dec_threads(c);
+  return dec_ctas_per_sm(t, dec_smem_layout(c, cols, true, false, false)) >=
+         dec_ctas_per_sm(t, dec_smem_layout(c, cols, false, false, false));
+}
+
+size_t dec_smem_bytes(const sqg_circuit* c, int cols, bool z_in_smem, bool adam = false) {
+  return dec_smem_layout(c, cols, dec_target_in_smem(c, cols), z_in_smem, adam);
+}
+
+constexpr size_t kDecSmemLimit = 110 * 1024;  // keep two CTAs per SM
 
 // Per-instance BFGS matrices stay in shared memory only while they are small (<= 16 KB) and
 // cost no resident CTA: beyond that, keeping them in the caller's workspace (L2-resident for
@@ -826,7 +849,7 @@ int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, v
 // Evaluation form of the decomposition kernels for this circuit and target width.
 void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
   a.has_lam = dec_needs_lam(c, cols) ? 1 : 0;
-  a.tgt_in_smem = dec_target_in_smem(c) ? 1 : 0;
+  a.tgt_in_smem = dec_target_in_smem(c, cols) ? 1 : 0;
   a.inv_cols = 1.0 / cols;
   a.cyclic = use_cyclic(c, cols) ? 1 : 0;
   a.chains = 1;
