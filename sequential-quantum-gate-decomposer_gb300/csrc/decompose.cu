@@ -730,15 +730,18 @@ size_t dec_smem_layout(const sqg_circuit* c, int cols, bool tgt, bool z, bool ad
 // memory each: the smaller of the shared-memory and the register limit (80 registers a thread,
 // as __launch_bounds__ fixes them).
 int dec_ctas_per_sm(int threads, size_t smem) {
-  static int per_sm = -1, reserved = 1024;
-  if (per_sm < 0) {
+  struct SmemAttrs {
+    size_t per_sm = 228 * 1024, reserved = 1024;
+  };
+  static const SmemAttrs attrs = [] {  // thread-safe one-time initialisation
+    SmemAttrs a;
     int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    per_sm = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess ? v
-                                                                                                       : 228 * 1024;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess) reserved = v;
-  }
-  const size_t by_smem = (size_t)per_sm / (smem + (size_t)reserved);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess) a.per_sm = v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess) a.reserved = v;
+    return a;
+  }();
+  const size_t by_smem = attrs.per_sm / (smem + attrs.reserved);
   const size_t by_regs = 65536 / (80 * (size_t)threads);
   return (int)std::min(by_smem, by_regs);
 }
