@@ -275,6 +275,23 @@ int sqg_decompose_batched_adam(const sqg_circuit* circuit, const void* targets_d
                                int random_shift_count_max, long long randomization_threshold, int max_outer,
                                unsigned long long seed, void* stream);
 
+/* Batched ADAM decompositions of many gate STRUCTURES at once: sqg_decompose_structures with
+ * the engine of sqg_decompose_batched_adam, the optimizer the structure-search decomposers use
+ * above five qubits (N_Qubit_Decomposition_Tree_Search.cpp:1487-1495 sets ADAM with
+ * max_inner_iterations P / 852 * 1e7 and random_shift_count_max 5 for each candidate's
+ * N_Qubit_Decomposition_custom).  Instance b decomposes with gate list gates[b * gate_num ..),
+ * checked against `circuit` as in sqg_decompose_structures, target targets_dev + b *
+ * target_stride (0: one shared target), random numbers seeded with seed + 7919 b; otherwise as
+ * sqg_decompose_batched_adam.  The workspace (256-byte aligned,
+ * sqg_decompose_structures_adam_workspace_bytes) holds the staged gate lists. */
+size_t sqg_decompose_structures_adam_workspace_bytes(const sqg_circuit* circuit, int batch);
+int sqg_decompose_structures_adam(const sqg_circuit* circuit, const sqg_gate* gates, const void* targets_dev,
+                                  long long target_stride, int cols, int batch, int trace_offset, int cost_variant,
+                                  double* x_dev, double* cost_dev, int* evals_dev, int* shifts_dev, double tolerance,
+                                  int max_iters, double eta, int adaptive_eta, int random_shift_count_max,
+                                  long long randomization_threshold, int max_outer, unsigned long long seed,
+                                  void* workspace_dev, size_t workspace_bytes, void* stream);
+
 /* One decomposition with SQUANDER's ADAM engine for any qbit_num the gradient supports
  * (<= 12), run on the device as a single CUDA graph launch: a conditional while-node whose
  * body evaluates the cost and gradient (the kernels of sqg_cost_grad) and then takes one

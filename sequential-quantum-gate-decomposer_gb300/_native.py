@@ -143,6 +143,11 @@ def _declare(lib):
                                              vp]
     lib.sqg_decompose_batched.argtypes = [vp, vp, c_int, c_int, c_int, c_int, vp, vp, vp, vp, ctypes.c_double,
                                           c_int, c_int, c_int, c_int, ctypes.c_ulonglong, vp, c_sz, vp]
+    lib.sqg_decompose_structures_adam_workspace_bytes.restype = c_sz
+    lib.sqg_decompose_structures_adam_workspace_bytes.argtypes = [vp, c_int]
+    lib.sqg_decompose_structures_adam.argtypes = [vp, vp, vp, c_ll, c_int, c_int, c_int, c_int, vp, vp, vp, vp,
+                                                  ctypes.c_double, c_int, ctypes.c_double, c_int, c_int, c_ll, c_int,
+                                                  ctypes.c_ulonglong, vp, c_sz, vp]
 
 
 def lib():
@@ -187,7 +192,7 @@ EXPORTED_SYMBOLS = [
     "sqg_apply_from_right", "sqg_combined_unitary", "sqg_decompose_workspace_bytes", "sqg_decompose_batched", "sqg_decompose_batched_adam",
     "sqg_adam_loop_workspace_bytes", "sqg_decompose_adam_loop", "sqg_decompose_structures_workspace_bytes",
     "sqg_bfgs_loop_workspace_bytes", "sqg_decompose_bfgs_loop",
-    "sqg_decompose_structures",
+    "sqg_decompose_structures", "sqg_decompose_structures_adam_workspace_bytes", "sqg_decompose_structures_adam",
     "sqg_state_workspace_bytes", "sqg_state_block_count", "sqg_apply_state", "sqg_circuit_set_partitions",
     "sqg_probe_fp64_scratch_bytes", "sqg_probe_fp64_tflops",
     "sqg_mlp_gemm_bf16", "sqg_mlp_to_bf16", "sqg_mlp_relu_backward", "sqg_mlp_col_sum", "sqg_mlp_adam",

@@ -863,6 +863,31 @@ void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
   }
 }
 
+// Checks batch gate lists against the circuit (the same gate types and parameter layout; only
+// target and control qubits may differ, in range and distinct) and stages them at dst on the
+// device, so that the kernel indexes in range.  Returns SQG_OK or the error status.
+int stage_gate_lists(const sqg_circuit* c, const sqg_gate* gates, int batch, Gate* dst, void* stream) {
+  const int L = c->L, n = c->n;
+  std::vector<Gate> lists((size_t)batch * L);
+  for (long long b = 0; b < batch; b++)
+    for (int g = 0; g < L; g++) {
+      const sqg_gate& in = gates[b * L + g];
+      const Gate& t = c->h_gates[g];
+      const bool ctl = gate_controlled(t.type);
+      if (in.type != t.type || in.param_start != t.pstart)
+        return set_error(SQG_ERR_INVALID_ARGUMENT, "gate list " + std::to_string(b) + " differs from the circuit's gate "
+                                                       "types or parameter layout at gate " + std::to_string(g));
+      if (in.target < 0 || in.target >= n || (ctl && (in.control < 0 || in.control >= n || in.control == in.target)))
+        return set_error(SQG_ERR_INVALID_ARGUMENT, "gate list " + std::to_string(b) + ": qubit out of range at gate " +
+                                                       std::to_string(g));
+      lists[b * L + g] = Gate{in.type, in.target, ctl ? in.control : -1, in.param_start};
+    }
+  // pageable source: the call returns once the records are staged, so `lists` may go
+  cudaError_t e = cudaMemcpyAsync(dst, lists.data(), sizeof(Gate) * lists.size(), cudaMemcpyHostToDevice,
+                                  (cudaStream_t)stream);
+  return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("gate lists: ") + cudaGetErrorString(e));
+}
+
 }  // namespace
 
 namespace sqg {
@@ -986,29 +1011,10 @@ int sqg_decompose_structures(const sqg_circuit* c, const sqg_gate* gates, const 
   const size_t need = sqg_decompose_structures_workspace_bytes(c, batch, cols);
   if (!workspace || ws_bytes < need || ((size_t)workspace & 255))
     return set_error(SQG_ERR_WORKSPACE, "workspace too small or not 256-byte aligned: need " + std::to_string(need));
-  // every gate list repeats the template's gate types and parameter layout; only the qubits
-  // may differ, and they are checked here so that the kernel indexes in range
   const int L = c->L, n = c->n;
-  std::vector<Gate> lists((size_t)batch * L);
-  for (long long b = 0; b < batch; b++)
-    for (int g = 0; g < L; g++) {
-      const sqg_gate& in = gates[b * L + g];
-      const Gate& t = c->h_gates[g];
-      const bool ctl = gate_controlled(t.type);
-      if (in.type != t.type || in.param_start != t.pstart)
-        return set_error(SQG_ERR_INVALID_ARGUMENT, "gate list " + std::to_string(b) + " differs from the circuit's gate "
-                                                       "types or parameter layout at gate " + std::to_string(g));
-      if (in.target < 0 || in.target >= n || (ctl && (in.control < 0 || in.control >= n || in.control == in.target)))
-        return set_error(SQG_ERR_INVALID_ARGUMENT, "gate list " + std::to_string(b) + ": qubit out of range at gate " +
-                                                       std::to_string(g));
-      lists[b * L + g] = Gate{in.type, in.target, ctl ? in.control : -1, in.param_start};
-    }
   const size_t zbytes = zs ? 0 : ((size_t)batch * c->P * c->P * sizeof(double) + 255) / 256 * 256;
   Gate* dgates = (Gate*)((char*)workspace + zbytes);
-  // pageable source: the call returns once the records are staged, so `lists` may go
-  cudaError_t e = cudaMemcpyAsync(dgates, lists.data(), sizeof(Gate) * lists.size(), cudaMemcpyHostToDevice,
-                                  (cudaStream_t)stream);
-  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("gate lists: ") + cudaGetErrorString(e));
+  if (int st = stage_gate_lists(c, gates, batch, dgates, stream)) return st;
   DecArgs a = {};
   a.gates = dgates;
   a.gstride = L;
@@ -1053,6 +1059,61 @@ int sqg_decompose_batched_adam(const sqg_circuit* c, const void* targets, int co
   a.variant = cost_variant;
   a.targets = (const double2*)targets;
   a.tstride = (long long)c->N * cols;
+  a.x = x; a.cost = cost; a.calls = evals; a.iters = shifts;
+  a.B = batch;
+  a.tol = tolerance;
+  a.max_calls = max_iters; a.max_outer = max_outer; a.loops = 1;
+  a.early_stop = 1;
+  a.seed = seed;
+  a.zglob = nullptr;
+  a.z_in_smem = 0;
+  a.eta = eta;
+  a.adaptive_eta = adaptive_eta ? 1 : 0;
+  a.shift_max = random_shift_count_max;
+  a.rand_thr = randomization_threshold;
+  dec_eval_form(c, cols, off, a);
+  return dec_launch<kAdam>(c, a, batch, smem, stream);
+}
+
+size_t sqg_decompose_structures_adam_workspace_bytes(const sqg_circuit* c, int batch) {
+  if (!c || batch <= 0) return 0;
+  return (size_t)batch * std::max(c->L, 1) * sizeof(Gate) + 256;
+}
+
+int sqg_decompose_structures_adam(const sqg_circuit* c, const sqg_gate* gates, const void* targets,
+                                  long long target_stride, int cols, int batch, int trace_offset, int cost_variant,
+                                  double* x, double* cost, int* evals, int* shifts, double tolerance, int max_iters,
+                                  double eta, int adaptive_eta, int random_shift_count_max,
+                                  long long randomization_threshold, int max_outer, unsigned long long seed,
+                                  void* workspace, size_t ws_bytes, void* stream) {
+  if (!c || !gates || !targets || !x || !cost || !evals || batch <= 0 || batch > 0x7fffffff / 2 || cols <= 0 ||
+      cols > c->N)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "bad circuit, gate lists, batch, targets or outputs");
+  if (c->P == 0) return set_error(SQG_ERR_INVALID_ARGUMENT, "the circuit has no free parameters");
+  if (cost_variant != SQG_FROBENIUS_NORM && cost_variant != SQG_HILBERT_SCHMIDT_TEST && cost_variant != SQG_INFIDELITY)
+    return set_error(SQG_ERR_UNSUPPORTED, "cost function variant not implemented by the engine");
+  const int off = cost_variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
+  if (off < 0 || off + cols > c->N) return set_error(SQG_ERR_INVALID_ARGUMENT, "trace offset out of range");
+  if (c->n > 6) return set_error(SQG_ERR_UNSUPPORTED, "batched decomposition keeps a whole target per CTA: qbit_num <= 6");
+  if (max_iters < 1 || max_outer < 1 || random_shift_count_max < 0 || randomization_threshold < 0)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "iteration limits must be positive");
+  if (target_stride != 0 && target_stride < (long long)c->N * cols)
+    return set_error(SQG_ERR_INVALID_ARGUMENT, "target stride must be 0 (one shared target) or at least rows * cols");
+  const size_t smem = dec_smem_bytes(c, cols, false, true);
+  if (smem > 227 * 1024) return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
+  const size_t need = sqg_decompose_structures_adam_workspace_bytes(c, batch);
+  if (!workspace || ws_bytes < need || ((size_t)workspace & 255))
+    return set_error(SQG_ERR_WORKSPACE, "workspace too small or not 256-byte aligned: need " + std::to_string(need));
+  Gate* dgates = (Gate*)workspace;
+  if (int st = stage_gate_lists(c, gates, batch, dgates, stream)) return st;
+  DecArgs a = {};
+  a.gates = dgates;
+  a.gstride = c->L;
+  a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N; a.cols = cols;
+  a.trace_offset = off;
+  a.variant = cost_variant;
+  a.targets = (const double2*)targets;
+  a.tstride = target_stride;
   a.x = x; a.cost = cost; a.calls = evals; a.iters = shifts;
   a.B = batch;
   a.tol = tolerance;

@@ -232,12 +232,51 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
             st.synchronize()
         return [self._collect(res) for res, _keep in launched]
 
+    # structures per level from which six-qubit ADAM decompositions run one CTA each in a single
+    # launch (sqg_decompose_structures_adam) instead of one whole-GPU graph launch per structure
+    batch_adam_min = 4
+
+    def _launch_structures_adam(self, codes, tol, iters, target):
+        """One launch of ADAM decompositions of the structures of `codes` (six qubits at most),
+        one CTA each.  Returns (x, cost, evals) on the device and the buffers that must outlive
+        the launch."""
+        n, topo = self.qbit_num, self.topology
+        nc = structure_circuit(codes[0], topo, n).native()
+        P, B = nc.param_num, codes.shape[0]
+        lib = _native.lib()
+        recs = np.ascontiguousarray(structure_records(codes, topo, n))
+        x = dev.to_device_real(self.rng.uniform(0.0, 2 * math.pi, (B, P)))
+        cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
+        evals = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
+        w = dev.Workspace().get(lib.sqg_decompose_structures_adam_workspace_bytes(nc.handle, B))
+        _native.check(lib.sqg_decompose_structures_adam(
+            nc.handle, recs.ctypes.data, dev.ptr(target), 0, target.shape[1], B, self.trace_offset,
+            self.cost_variant, dev.ptr(x), dev.ptr(cost), dev.ptr(evals), None, tol, iters, 1e-3, 1, 5, 2500000, 1,
+            int(self.rng.integers(1 << 62)), dev.ptr(w), w.numel(), dev.stream_ptr()),
+            "sqg_decompose_structures_adam")
+        return (x, cost, evals), (nc, w)
+
     def _decompose_level_large(self, codes, tol, target):
         """ADAM decompositions (the reference's choice above five qubits: max_inner_iterations
-        P / 852 * 1e7, random_shift_count_max 5, :1487-1495), one graph launch per structure."""
+        P / 852 * 1e7, random_shift_count_max 5, :1487-1495).  At six qubits a level of at least
+        batch_adam_min structures runs in launches of `chunk` structures, one CTA each, stopping
+        after the first launch that reaches the tolerance (as the BFGS levels below six qubits);
+        otherwise one graph launch per structure, stopping at the first that reaches it."""
         n, topo = self.qbit_num, self.topology
         best = (math.inf, -1, None)
         evals = 0
+        if n <= 6 and codes.shape[0] >= self.batch_adam_min:
+            P = structure_circuit(codes[0], topo, n).get_Parameter_Num()
+            iters = max(1, int(P / 852 * 10000000.0))
+            for s in range(0, codes.shape[0], self.chunk):
+                res, _keep = self._launch_structures_adam(codes[s:s + self.chunk], tol, iters, target)
+                f, k, x, ev = self._collect(res, s)
+                evals += ev
+                if f < best[0]:
+                    best = (f, k, x)
+                if best[0] < tol:
+                    break
+            return best[0], best[1], best[2], evals
         for i, code in enumerate(codes):
             circ = structure_circuit(code, topo, n)
             P = circ.get_Parameter_Num()

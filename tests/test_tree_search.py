@@ -207,6 +207,58 @@ def test_structures_with_per_instance_targets(sqg, ts):
 
 
 @pytest.mark.gpu
+def test_structures_adam_equal_single_structure_runs(sqg, ts):
+    """Six-qubit structures with SQUANDER's ADAM engine in one launch (the optimizer the
+    structure searches use above five qubits), one CTA per structure: every instance equals,
+    bit for bit, a batched ADAM run of its own structure (same CTA index, so the same random
+    stream seed + 7919 b)."""
+    torch = pytest.importorskip("torch")
+    lib = importlib.import_module("sequential-quantum-gate-decomposer_gb300._native")
+    n = 6
+    topo = ts.normalize_topology(None, n)
+    codes = ts.level_codes(1, topo)[:5]
+    B = codes.shape[0]
+    rng = np.random.default_rng(8)
+    circs = [ts.structure_circuit(codes[k], topo, n) for k in range(B)]
+    P = circs[0].get_Parameter_Num()
+    T = np.stack([np.ascontiguousarray(O.get_matrix(n, circs[k].gate_records(),
+                                                    rng.uniform(0, 2 * np.pi, P)).conj().T) for k in range(B)])
+    x0 = rng.uniform(0, 2 * np.pi, (B, P))
+    nc = circs[0].native()
+    recs = np.ascontiguousarray(ts.structure_records(codes, topo, n))
+    t = torch.from_numpy(T).cuda()
+    x = torch.from_numpy(x0.copy()).cuda()
+    cost = torch.empty(B, dtype=torch.float64, device="cuda")
+    evals = torch.empty(B, dtype=torch.int32, device="cuda")
+    shifts = torch.empty(B, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.lib().sqg_decompose_structures_adam_workspace_bytes(nc.handle, B), dtype=torch.uint8,
+                     device="cuda")
+    lib.check(lib.lib().sqg_decompose_structures_adam(
+        nc.handle, recs.ctypes.data, t.data_ptr(), 64 * 64, 64, B, 0, 0, x.data_ptr(), cost.data_ptr(),
+        evals.data_ptr(), shifts.data_ptr(), 1e-8, 40, 1e-3, 1, 5, 2500000, 1, 5, ws.data_ptr(), ws.numel(),
+        torch.cuda.current_stream().cuda_stream), "structures_adam")
+    torch.cuda.synchronize()
+    assert np.all(evals.cpu().numpy() == 40)
+    for k in range(B):
+        dec = sqg.BatchedDecomposer(circs[k], tolerance=1e-8, max_calls=40, max_outer=1, optimizer="ADAM", eta=1e-3,
+                                    random_shift_count_max=5)
+        xk, ck, ek = dec.run(T, x0, seed=5)
+        torch.cuda.synchronize()
+        assert float(ck[k]) == float(cost[k]) and torch.equal(xk[k], x[k]) and int(ek[k]) == int(evals[k])
+    bad = recs.copy()
+    bad[0, -1, 1] = n
+    assert lib.lib().sqg_decompose_structures_adam(
+        nc.handle, bad.ctypes.data, t.data_ptr(), 64 * 64, 64, B, 0, 0, x.data_ptr(), cost.data_ptr(),
+        evals.data_ptr(), None, 1e-8, 40, 1e-3, 1, 5, 2500000, 1, 5, ws.data_ptr(), ws.numel(),
+        torch.cuda.current_stream().cuda_stream) == 1
+    assert lib.lib().sqg_decompose_structures_adam(
+        nc.handle, recs.ctypes.data, t.data_ptr(), 64 * 64, 64, B, 0, 0, x.data_ptr(), cost.data_ptr(),
+        evals.data_ptr(), None, 1e-8, 40, 1e-3, 1, 5, 2500000, 1, 5, ws.data_ptr(), 64,
+        torch.cuda.current_stream().cuda_stream) == 3
+    torch.cuda.synchronize()
+
+
+@pytest.mark.gpu
 def test_tree_search_on_a_linear_topology(sqg, ts):
     """Four qubits on a line (0-1, 1-2, 2-3): commuting CNOTs on disjoint pairs are enumerated
     once; a target from two such CNOTs is found at level 2."""
