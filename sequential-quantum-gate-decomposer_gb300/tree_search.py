@@ -236,6 +236,12 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
     # launch (sqg_decompose_structures_adam) instead of one whole-GPU graph launch per structure
     batch_adam_min = 4
 
+    @staticmethod
+    def _adam_budget(P):
+        """ADAM evaluations per candidate above five qubits (max_inner_iterations P / 852 * 1e7,
+        N_Qubit_Decomposition_Tree_Search.cpp:1487-1495)."""
+        return max(1, int(P / 852 * 10000000.0))
+
     def _launch_structures_adam(self, codes, tol, iters, target):
         """One launch of ADAM decompositions of the structures of `codes` (six qubits at most),
         one CTA each.  Returns (x, cost, evals) on the device and the buffers that must outlive
@@ -266,8 +272,7 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
         best = (math.inf, -1, None)
         evals = 0
         if n <= 6 and codes.shape[0] >= self.batch_adam_min:
-            P = structure_circuit(codes[0], topo, n).get_Parameter_Num()
-            iters = max(1, int(P / 852 * 10000000.0))
+            iters = self._adam_budget(structure_circuit(codes[0], topo, n).get_Parameter_Num())
             for s in range(0, codes.shape[0], self.chunk):
                 res, _keep = self._launch_structures_adam(codes[s:s + self.chunk], tol, iters, target)
                 f, k, x, ev = self._collect(res, s)
@@ -280,7 +285,7 @@ class N_Qubit_Decomposition_Tree_Search(N_Qubit_Decomposition_custom):
         for i, code in enumerate(codes):
             circ = structure_circuit(code, topo, n)
             P = circ.get_Parameter_Num()
-            iters = max(1, int(P / 852 * 10000000.0))
+            iters = self._adam_budget(P)
             x, cost, ev, _ = adam_decompose_graph(circ, target, self.rng.uniform(0.0, 2 * math.pi, P), tol, iters,
                                                   random_shift_count_max=5, seed=int(self.rng.integers(1 << 62)),
                                                   trace_offset=self.trace_offset, cost_variant=self.cost_variant)

@@ -259,6 +259,32 @@ def test_structures_adam_equal_single_structure_runs(sqg, ts):
 
 
 @pytest.mark.gpu
+def test_six_qubit_level_runs_as_one_adam_structure_batch(sqg, ts, monkeypatch):
+    """A six-qubit level of five candidates goes through one sqg_decompose_structures_adam
+    launch (budget shrunk from the reference's P / 852 * 1e7 for the test); a single candidate
+    goes through the graph-driven ADAM loop."""
+    torch = pytest.importorskip("torch")
+    n = 6
+    topo = ts.normalize_topology(None, n)
+    codes = ts.level_codes(1, topo)[:5]
+    rng = np.random.default_rng(9)
+    c = ts.structure_circuit(codes[2], topo, n)
+    U = O.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
+    dec = sqg.N_Qubit_Decomposition_Tree_Search(np.ascontiguousarray(U.conj().T),
+                                                config={"optimization_tolerance": 1e-8, "random_seed": 4})
+    monkeypatch.setattr(ts.N_Qubit_Decomposition_Tree_Search, "_adam_budget", staticmethod(lambda P: 30))
+    target = dec.evaluator().target
+    f, k, x, evals = dec._decompose_level_large(codes, 1e-8, target)
+    torch.cuda.synchronize()
+    assert 0 <= k < 5 and np.isfinite(f) and x.shape == (c.get_Parameter_Num(),)
+    assert evals == 5 * 30  # none reaches 1e-8 in 30 ADAM steps: every candidate runs its budget
+    assert abs(O.cost(n, ts.structure_circuit(codes[k], topo, n).gate_records(), x,
+                      np.ascontiguousarray(U.conj().T)) - f) < 1e-10
+    f1, k1, x1, ev1 = dec._decompose_level_large(codes[:1], 1e-8, target)
+    assert k1 == 0 and ev1 == 30 and np.isfinite(f1)
+
+
+@pytest.mark.gpu
 def test_tree_search_on_a_linear_topology(sqg, ts):
     """Four qubits on a line (0-1, 1-2, 2-3): commuting CNOTs on disjoint pairs are enumerated
     once; a target from two such CNOTs is found at level 2."""
