@@ -299,3 +299,12 @@ def test_tree_search_on_a_linear_topology(sqg, ts):
     assert dec.get_Decomposition_Error() < 1e-8
     assert len(dec.best_cnot_sequence) <= 2
     assert all(p in topo for p in dec.best_cnot_sequence)
+
+
+def test_adam_budget_above_five_qubits_follows_the_reference(ts):
+    """The ADAM budget per candidate is SQUANDER's static_cast<int>(P / 852 * 1e7)
+    (N_Qubit_Decomposition_Tree_Search.cpp:1487-1495), at least one evaluation."""
+    cls = ts.N_Qubit_Decomposition_Tree_Search
+    assert cls._adam_budget(852) == 10000000
+    assert cls._adam_budget(36) == int(36 / 852 * 10000000.0) == 422535
+    assert cls._adam_budget(0) == 1
