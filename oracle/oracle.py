@@ -57,6 +57,8 @@ def lib():
         _lib.sqgo_cost.argtypes = [i, ip, i, dp, i, dp, i, i, i, dp]
         _lib.sqgo_cost_grad.argtypes = [i, ip, i, dp, i, dp, i, i, i, dp, dp]
         _lib.sqgo_batch.argtypes = [i, ip, i, dp, i, i, dp, i, i, i, i, dp, dp, i]
+        _lib.sqgo_batch2.argtypes = [i, ip, i, dp, i, i, dp, i, i, i, i, dp, dp, i, i]
+        _lib.sqgo_cost_grad_sweep.argtypes = [i, ip, i, dp, i, dp, i, i, i, dp, dp]
         _lib.sqgo_decompose.argtypes = [i, ip, i, i, dp, i, i, i, dp, ctypes.c_double, ctypes.c_long, i, i,
                                         ctypes.c_uint64, dp, lp]
         _lib.sqgo_decompose_batch.argtypes = [i, ip, i, i, i, dp, i, i, i, dp, ctypes.c_double, ctypes.c_long, i,
@@ -147,9 +149,23 @@ def cost_grad(qbit_num, gates, params, target, trace_offset=0, variant=FROBENIUS
     return float(out[0]), grad[:p.size].copy()
 
 
-def batch(qbit_num, gates, params, target, trace_offset=0, variant=FROBENIUS_NORM, with_grad=False, nthreads=None):
+def cost_grad_sweep(qbit_num, gates, params, target, trace_offset=0, variant=FROBENIUS_NORM):
+    """cost_grad by the reverse sweep (three matrices instead of P derivative matrices)."""
+    g, gp, L = _gates(gates)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    t = np.ascontiguousarray(target, dtype=np.complex128)
+    out = np.zeros(1)
+    grad = np.zeros(max(p.size, 1))
+    _check(lib().sqgo_cost_grad_sweep(qbit_num, gp, L, _dp(p), p.size, _dp(t.view(np.float64)), t.shape[1],
+                                      trace_offset, variant, _dp(out), _dp(grad)), "cost_grad_sweep")
+    return float(out[0]), grad[:p.size].copy()
+
+
+def batch(qbit_num, gates, params, target, trace_offset=0, variant=FROBENIUS_NORM, with_grad=False, nthreads=None,
+          sweep=False):
     """Costs (and gradients) of B parameter rows; target is (rows, cols) shared or
-    (B, rows, cols) per instance."""
+    (B, rows, cols) per instance.  sweep=True computes the gradients by the reverse sweep
+    (sqgo_cost_grad_sweep), for sizes whose P derivative matrices do not fit in memory."""
     g, gp, L = _gates(gates)
     p = np.ascontiguousarray(params, dtype=np.float64)
     B, P = p.shape
@@ -159,8 +175,9 @@ def batch(qbit_num, gates, params, target, trace_offset=0, variant=FROBENIUS_NOR
     costs = np.zeros(B)
     grads = np.zeros((B, max(P, 1))) if with_grad else None
     nthreads = nthreads or os.cpu_count() or 1
-    _check(lib().sqgo_batch(qbit_num, gp, L, _dp(p), P, B, _dp(t.view(np.float64)), cols, per, trace_offset, variant,
-                            _dp(costs), _dp(grads) if with_grad else None, nthreads), "batch")
+    _check(lib().sqgo_batch2(qbit_num, gp, L, _dp(p), P, B, _dp(t.view(np.float64)), cols, per, trace_offset,
+                             variant, _dp(costs), _dp(grads) if with_grad else None, nthreads, 1 if sweep else 0),
+           "batch")
     return (costs, grads[:, :P]) if with_grad else costs
 
 

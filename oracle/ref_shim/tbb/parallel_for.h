@@ -1,0 +1,2 @@
+/* ORACLE build support: see tbb.h */
+#include "tbb.h"

@@ -392,9 +392,114 @@ int sqgo_cost_grad(int qbit_num, const sqgo_gate* g, int L, const double* params
   return rc;
 }
 
+/* ---------------- gradient by a reverse sweep (sizes the prefix form cannot hold) -----
+ * The reference materialises all P derivative matrices (Gates_block.cpp:1012-1150),
+ * which needs P * 16 * rows * cols bytes: 30 GB at 10 qubits with 1830 parameters.  This
+ * is the same gradient, organised so that it needs three matrices:
+ *   t_p = sum_{i<cols} (S_j dG_j P_j)[i + off, i] = sum_{i, a, b} R_j[i, a] dG_j[a, b] P_j[b, i]
+ * with P_j = G_{j-1}..G_0 T (rows x cols, the input of gate j) and R_j = E G_{L-1}..G_{j+1}
+ * (cols x rows, E selecting rows off..off+cols-1).  The sweep starts from W = C T and
+ * R = E and walks the gates backwards: P_j = G_j^dagger P_{j+1} (uncomputation, exact up
+ * to rounding because the gates are unitary), R_{j-1} = R_j G_j.  dG_j is the derivative
+ * kernel with the reference's zeroing of uncontrolled row pairs (apply_kernel_to_input.cpp:93-97).
+ * The gradient formulas are those of sqgo_cost_grad.  It agrees with the prefix form to
+ * rounding; the tests check both against the reference where both fit in memory. */
+static void kernel_dagger(const double* k, double* kd) {
+  kd[0] = k[0]; kd[1] = -k[1]; kd[2] = k[4]; kd[3] = -k[5];
+  kd[4] = k[2]; kd[5] = -k[3]; kd[6] = k[6]; kd[7] = -k[7];
+}
+
+/* sum_i sum_{a,b} R[i,a] D[a,b] P[b,i] for the embedded derivative kernel D of one gate */
+static void deriv_contract(const double* R, const double* Pm, int rows, int cols, const double* k, int target,
+                           int control, double* out_r, double* out_i) {
+  const int step = 1 << target;
+  double sr = 0.0, si = 0.0;
+  for (int base = 0; base + step < rows; base += step << 1) {
+    for (int idx = 0; idx < step; idx++) {
+      int r0 = base + idx, r1 = r0 + step;
+      if (control >= 0 && !((r0 >> control) & 1)) continue;
+      const double* p0 = Pm + 2L * r0 * cols;
+      const double* p1 = Pm + 2L * r1 * cols;
+      for (int i = 0; i < cols; i++) {
+        double ar = p0[2 * i], ai = p0[2 * i + 1], br = p1[2 * i], bi = p1[2 * i + 1];
+        /* (D P)[r0, i] and (D P)[r1, i] */
+        double xr = k[0] * ar - k[1] * ai + k[2] * br - k[3] * bi;
+        double xi = k[0] * ai + k[1] * ar + k[2] * bi + k[3] * br;
+        double yr = k[4] * ar - k[5] * ai + k[6] * br - k[7] * bi;
+        double yi = k[4] * ai + k[5] * ar + k[6] * bi + k[7] * br;
+        const double* q = R + 2L * i * rows;
+        double u0r = q[2 * r0], u0i = q[2 * r0 + 1], u1r = q[2 * r1], u1i = q[2 * r1 + 1];
+        sr += u0r * xr - u0i * xi + u1r * yr - u1i * yi;
+        si += u0r * xi + u0i * xr + u1r * yi + u1i * yr;
+      }
+    }
+  }
+  *out_r = sr;
+  *out_i = si;
+}
+
+int sqgo_cost_grad_sweep(int qbit_num, const sqgo_gate* g, int L, const double* params, int P, const double* target,
+                         int cols, int trace_offset, int variant, double* cost, double* grad) {
+  int rows = 1 << qbit_num;
+  int rc = check_gates(qbit_num, g, L, P);
+  if (rc) return rc;
+  size_t msz = (size_t)rows * cols * 2;
+  double* Pm = (double*)malloc(sizeof(double) * msz);
+  double* R = (double*)calloc(msz, sizeof(double));
+  memcpy(Pm, target, sizeof(double) * msz);
+  rc = sqgo_apply_to(qbit_num, g, L, params, P, Pm, rows, cols, cols);
+  if (rc) { free(Pm); free(R); return rc; }
+  *cost = sqgo_cost_of_matrix(Pm, cols, cols, trace_offset, variant);
+  double tr = 0, ti = 0;
+  if (variant != FROBENIUS_NORM) complex_trace(Pm, cols, cols, &tr, &ti);
+  const int off = variant == FROBENIUS_NORM ? trace_offset : 0;
+  for (int i = 0; i < cols; i++) R[2L * ((size_t)i * rows + i + off)] = 1.0;
+  double* sc = precompute_sincos(params, P);
+  for (int j = L - 1; j >= 0; j--) {
+    const sqgo_gate* gj = &g[j];
+    double k[8], kd[8];
+    /* P <- G_j^dagger P */
+    switch (gj->type) {
+      case T_CNOT: apply_x(Pm, rows, cols, cols, gj->target, gj->control); break;
+      case T_CZ: apply_z(Pm, rows, cols, cols, gj->target, gj->control); break;
+      default:
+        gate_kernel(gj->type, sc + 2 * gj->param_start, -1, k);
+        kernel_dagger(k, kd);
+        apply_kernel(Pm, rows, cols, cols, kd, gj->target, gj->type == T_CRY ? gj->control : -1, 0);
+    }
+    int pn = param_num(gj->type);
+    for (int p = 0; p < pn; p++) {
+      double dk[8], dr, di;
+      gate_kernel(gj->type, sc + 2 * gj->param_start, p, dk);
+      deriv_contract(R, Pm, rows, cols, dk, gj->target, gj->type == T_CRY ? gj->control : -1, &dr, &di);
+      double* gp = &grad[gj->param_start + p];
+      if (variant == FROBENIUS_NORM) {
+        *gp = (1.0 - dr / cols) - 1.0;
+      } else if (variant == HILBERT_SCHMIDT_TEST) {
+        double dd = 1.0 / cols;
+        *gp = -2.0 * dd * dd * tr * dr - 2.0 * dd * dd * ti * di;
+      } else {
+        double dd = cols;
+        *gp = -2.0 / dd / (dd + 1) * tr * dr - 2.0 / dd / (dd + 1) * ti * di;
+      }
+    }
+    /* R <- R G_j */
+    switch (gj->type) {
+      case T_CNOT: apply_x_right(R, cols, rows, rows, gj->target, gj->control); break;
+      case T_CZ: apply_z_right(R, cols, rows, rows, gj->target, gj->control); break;
+      default:
+        apply_kernel_right(R, cols, rows, rows, k, gj->target, gj->type == T_CRY ? gj->control : -1);
+    }
+  }
+  free(sc);
+  free(Pm);
+  free(R);
+  return 0;
+}
+
 /* ---------------- thread-parallel batch (Optimization_Interface.cpp:940-1033) ------- */
 typedef struct {
-  int qbit_num, L, P, cols, trace_offset, variant, with_grad, B, tstride;
+  int qbit_num, L, P, cols, trace_offset, variant, with_grad, B, tstride, sweep;
   const sqgo_gate* g;
   const double* params;
   const double* target;
@@ -415,7 +520,10 @@ static void* batch_worker(void* arg) {
     if (b >= j->B) break;
     const double* tgt = j->target + (j->tstride ? tsz * b : 0);
     int rc;
-    if (j->with_grad)
+    if (j->with_grad && j->sweep)
+      rc = sqgo_cost_grad_sweep(j->qbit_num, j->g, j->L, j->params + (size_t)b * j->P, j->P, tgt, j->cols,
+                                j->trace_offset, j->variant, &j->cost[b], j->grad + (size_t)b * j->P);
+    else if (j->with_grad)
       rc = sqgo_cost_grad(j->qbit_num, j->g, j->L, j->params + (size_t)b * j->P, j->P, tgt, j->cols, j->trace_offset,
                           j->variant, &j->cost[b], j->grad + (size_t)b * j->P);
     else
@@ -427,15 +535,16 @@ static void* batch_worker(void* arg) {
 }
 
 /* Batched cost (and optional gradient) of B parameter vectors.  target_per_instance
- * selects one target per instance (B x rows x cols) instead of one shared target. */
-int sqgo_batch(int qbit_num, const sqgo_gate* g, int L, const double* params, int P, int B, const double* target,
-               int cols, int target_per_instance, int trace_offset, int variant, double* cost, double* grad,
-               int nthreads) {
+ * selects one target per instance (B x rows x cols) instead of one shared target; sweep
+ * selects the reverse-sweep gradient (sqgo_cost_grad_sweep) instead of the prefix form. */
+int sqgo_batch2(int qbit_num, const sqgo_gate* g, int L, const double* params, int P, int B, const double* target,
+                int cols, int target_per_instance, int trace_offset, int variant, double* cost, double* grad,
+                int nthreads, int sweep) {
   batch_job j;
   memset(&j, 0, sizeof(j));
   j.qbit_num = qbit_num; j.L = L; j.P = P; j.cols = cols; j.trace_offset = trace_offset; j.variant = variant;
   j.with_grad = grad != NULL; j.B = B; j.tstride = target_per_instance; j.g = g; j.params = params; j.target = target;
-  j.cost = cost; j.grad = grad;
+  j.cost = cost; j.grad = grad; j.sweep = sweep;
   pthread_mutex_init(&j.mu, NULL);
   if (nthreads < 1) nthreads = 1;
   pthread_t th[256];
@@ -444,6 +553,13 @@ int sqgo_batch(int qbit_num, const sqgo_gate* g, int L, const double* params, in
   for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
   pthread_mutex_destroy(&j.mu);
   return j.rc;
+}
+
+int sqgo_batch(int qbit_num, const sqgo_gate* g, int L, const double* params, int P, int B, const double* target,
+               int cols, int target_per_instance, int trace_offset, int variant, double* cost, double* grad,
+               int nthreads) {
+  return sqgo_batch2(qbit_num, g, L, params, P, B, target, cols, target_per_instance, trace_offset, variant, cost,
+                     grad, nthreads, 0);
 }
 
 /* ---------------- BFGS (Powell Z-matrix) decomposition driver ----------------------
@@ -619,15 +735,27 @@ static uint64_t splitmix(uint64_t* s) {
   return z ^ (z >> 31);
 }
 
+/* Counter-based uniform draw in [0, 1): the splitmix64 finaliser of k (53 random bits).
+ * The engine draws its restart perturbations the same way, so that decompositions with
+ * restarts can be compared draw for draw. */
+static double counter_u01(uint64_t k) {
+  uint64_t z = k + 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
 /* N_Qubit_Decomposition_custom::start_decomposition (N_Qubit_Decomposition_custom.cpp:116-190)
  * with BFGS (chosen for qbit_num <= 5, :59-76): up to max_outer outer iterations, each
  * running iteration_loops BFGS_Powell restarts (BFGS.cpp:121-150); after an improved
  * minimum the guess is perturbed by U[0, 2 pi)/100; the loop stops once the minimum is
- * below the tolerance (Decomposition_Base.cpp:742-752).  The perturbation stream is a
- * seeded splitmix64 (the reference draws from std::mt19937). */
+ * below the tolerance (Decomposition_Base.cpp:742-752).  The reference draws the
+ * perturbation from std::mt19937; here draw i of a perturbation is counter_u01(ctr + i),
+ * with ctr starting at `counter` and advancing by (P + 1) * (2^32 + 1) per perturbation. */
 int sqgo_decompose(int qbit_num, const sqgo_gate* g, int L, int P, const double* target, int cols, int trace_offset,
                    int variant, double* x, double tolerance, long max_inner, int max_outer, int iteration_loops,
-                   uint64_t seed, double* final_cost, long* total_calls) {
+                   uint64_t counter, double* final_cost, long* total_calls) {
   int rc = check_gates(qbit_num, g, L, P);
   if (rc) return rc;
   fg_ctx c = {qbit_num, L, P, cols, trace_offset, variant, g, target, 0};
@@ -635,7 +763,7 @@ int sqgo_decompose(int qbit_num, const sqgo_gate* g, int L, int P, const double*
   memcpy(guess, x, sizeof(double) * P);
   double best = INFINITY;
   long calls = 0;
-  uint64_t s = seed;
+  uint64_t ctr = counter;
   for (int outer = 0; outer < max_outer; outer++) {
     for (int loop = 0; loop < iteration_loops; loop++) {
       double f = bfgs_powell(&c, guess, max_inner);
@@ -643,7 +771,8 @@ int sqgo_decompose(int qbit_num, const sqgo_gate* g, int L, int P, const double*
       if (best > f) {
         best = f;
         memcpy(x, guess, sizeof(double) * P);
-        for (int i = 0; i < P; i++) guess[i] += (double)(splitmix(&s) >> 11) * (1.0 / 9007199254740992.0) * 2 * M_PI / 100;
+        for (int i = 0; i < P; i++) guess[i] = x[i] + counter_u01(ctr + (uint64_t)i) * (2 * M_PI) / 100.0;
+        ctr += 0x100000001ULL * (uint64_t)(P + 1);
       }
     }
     memcpy(guess, x, sizeof(double) * P);
@@ -679,7 +808,8 @@ static void* dec_worker(void* arg) {
     if (b >= j->B) break;
     sqgo_decompose(j->qbit_num, j->g, j->L, j->P, j->targets + tsz * b, j->cols, j->trace_offset, j->variant,
                    j->x + (size_t)b * j->P, j->tolerance, j->max_inner, j->max_outer, j->iteration_loops,
-                   j->seed + (uint64_t)b * 7919u, &j->cost[b], &j->calls[b]);
+                   j->seed * 0x2545F4914F6CDD1DULL + (uint64_t)b * 0x9E3779B97F4A7C15ULL, &j->cost[b],
+                   &j->calls[b]);
   }
   return NULL;
 }
