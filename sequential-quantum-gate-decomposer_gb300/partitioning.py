@@ -1,21 +1,39 @@
-"""Circuit partitioning: the step before the fused gate passes (squander/partitioning).
+"""Circuit partitioning: the step before the fused gate passes (squander.partitioning).
 
-Restates SQUANDER's greedy Kahn partitioner and its FLOP model:
-  build_dependency            squander/partitioning/tools.py:135-164
+Public functions and the reference functions whose results they reproduce:
   kahn_partition              squander/partitioning/kahn.py:7-78
   kahn_partition_preparts     squander/partitioning/kahn.py:81-165
-  split_partition             squander/partitioning/kahn.py:168-198
   get_float_ops               squander/partitioning/tools.py:26-45
   parts_to_float_ops          squander/partitioning/tools.py:48-81
   total_float_ops             squander/partitioning/tools.py:84-108
   translate_param_order       squander/partitioning/tools.py:111-132
   PartitionCircuit            squander/partitioning/partition.py:50-91
 
-The Kahn partitioner keeps the reference's data structures where they decide the result:
-the ready list is a binary heap of (sorted qubit tuple, gate index) that is scanned in its
-array order for the first gate that fits, entries are deleted by position and the heap is
-pushed to afterwards, and successor sets are iterated as Python sets.  The same input
-therefore gives the same partitions and parameter order as the reference.
+How the greedy partitioner decides, stated as the rules this module implements:
+
+1. The circuit's top-level items form a dependency graph (an item's successors are what
+   ``Circuit.get_Children`` returns).  Items whose predecessors have all been placed are
+   "ready".
+2. The ready items live in a binary min-heap (Python's heapq layout) keyed by (sorted tuple
+   of the item's qubits, item index).  The heap is not popped at its minimum: the
+   partitioner scans the heap's array from the front and takes the first item that the open
+   block admits, removing that array slot in place; items that become ready are then pushed
+   with heappush.  The heap's array order therefore decides ties, and this module keeps the
+   same array operations for that reason.
+3. The initial heap is built (heapify) from the sources listed in the iteration order of a
+   Python set of their indices; the items that become ready after an item is placed are
+   visited in the iteration order of a fresh Python set of its successors.
+4. A block admits an item while the union of their qubits has at most ``max_qubit`` qubits.
+   When the open block admits no ready item, it is closed and a new one opened.
+5. Each block is then split into its connected pieces (items joined by a direct dependency
+   inside the block).  Pieces are found in the order given by the first remaining element of
+   a Python set of the block's items, elements leaving the set one at a time.
+6. A second pass rebuilds the blocks: this time the open block admits exactly the items of
+   the next piece.  The second pass's blocks become the sub-circuits, and the parameter order
+   records where each item's parameters move.
+
+The result is identical to the reference's on the same circuit; the fixture
+tests/golden/partition_kahn.json, produced by running the reference's own modules, checks it.
 
 The ILP strategies ("ilp", "ilp-fusion", "ilp-fusion-ca") need the PuLP modelling package with
 the CBC or Gurobi solvers, and the "qiskit*" / "bqskit*" strategies need those frameworks; none
@@ -26,7 +44,6 @@ the state-vector plan then starts fused passes only at partition boundaries, mer
 consecutive partitions while they fit one shared-memory chunk (Circuit.native).
 """
 import heapq
-from itertools import dropwhile
 
 import numpy as np
 
@@ -38,157 +55,187 @@ def get_qubits(gate):
     return set(gate.get_Involved_Qbits())
 
 
-def build_dependency(c):
-    """(gate dict, successor sets, predecessor sets, qubit sets, start set) of the top-level
-    items of circuit c."""
-    gate_dict = {i: gate for i, gate in enumerate(c.get_Gates())}
-    gate_to_qubit = {i: get_qubits(g) for i, g in gate_dict.items()}
-    g, rg = {i: set() for i in gate_dict}, {i: set() for i in gate_dict}
-    for gate in gate_dict:
-        for child in c.get_Children(gate_dict[gate]):
-            g[gate].add(child)
-            rg[child].add(gate)
-    S = {m for m in rg if len(rg[m]) == 0}
-    return gate_dict, g, rg, gate_to_qubit, S
+class _Dag:
+    """Dependency graph of a circuit's top-level items."""
+
+    def __init__(self, circuit):
+        self.items = list(circuit.get_Gates())
+        count = len(self.items)
+        self.qubits = [frozenset(item.get_Involved_Qbits()) for item in self.items]
+        self.heap_key = [(tuple(sorted(q)), i) for i, q in enumerate(self.qubits)]
+        self.succ = [set() for _ in range(count)]
+        self.pred = [set() for _ in range(count)]
+        for i, item in enumerate(self.items):
+            for j in circuit.get_Children(item):
+                self.succ[i].add(j)
+                self.pred[j].add(i)
+
+    def sources(self):
+        """Indices without predecessors, as a set filled in index order (rule 3)."""
+        found = set()
+        for i, p in enumerate(self.pred):
+            if not p:
+                found.add(i)
+        return found
 
 
-def _kahn_walk(c, max_qubit, preparts, on_gate, on_close):
-    """The partitioner's topological walk: takes, from the ready heap in its array order,
-    the first gate that fits the open partition (at most max_qubit qubits, or membership in
-    the next predefined partition) and closes the partition when none fits.  on_gate(n,
-    gate) is called for every gate taken, on_close() when a partition is closed (also for
-    the last one).  Returns the list of partitions (lists of gate indices)."""
-    gate_dict, g, rg, gate_to_qubit, S = build_dependency(c)
-    S = [(tuple(sorted(gate_to_qubit[x])), x) for x in S]
-    heapq.heapify(S)
-    parts = [[]]
-    curr_partition = set()
+class _ReadyHeap:
+    """The ready items of rule 2: a heapq array scanned front to back."""
 
-    if preparts is None:
-        def partition_condition(idx):
-            return len(gate_to_qubit[S[idx][1]] | curr_partition) > max_qubit
-    else:
-        def partition_condition(idx):
-            return S[idx][1] not in preparts[len(parts) - 1]
+    def __init__(self, dag):
+        self._key = dag.heap_key
+        self._arr = [self._key[i] for i in dag.sources()]
+        heapq.heapify(self._arr)
 
-    total = 0
-    while S:
-        idx = next(dropwhile(partition_condition, range(len(S))), None)
-        if idx is None:  # the open partition cannot grow
-            on_close()
-            total += len(parts[-1])
-            curr_partition = set()
-            parts.append([])
-            idx = next(dropwhile(partition_condition, range(len(S))), None)
-            if idx is None:
+    def __len__(self):
+        return len(self._arr)
+
+    def take_first(self, admits):
+        for pos in range(len(self._arr)):
+            item = self._arr[pos][1]
+            if admits(item):
+                self._arr.pop(pos)
+                return item
+        return None
+
+    def push(self, item):
+        heapq.heappush(self._arr, self._key[item])
+
+
+def _greedy_blocks(dag, admits):
+    """Rules 2-4 (and 6 with a membership test): the blocks of item indices, in placement
+    order.  admits(block_number, block_qubits, item) says whether the open block takes item."""
+    ready = _ReadyHeap(dag)
+    waiting = [len(p) for p in dag.pred]
+    blocks = [[]]
+    block_qubits = set()
+    while len(ready):
+        item = ready.take_first(lambda i: admits(len(blocks) - 1, block_qubits, i))
+        if item is None:
+            blocks.append([])
+            block_qubits = set()
+            item = ready.take_first(lambda i: admits(len(blocks) - 1, block_qubits, i))
+            if item is None:
                 raise ValueError("a gate acts on more than max_partition_size qubits")
-        n = S[idx][1]
-        parts[-1].append(n)
-        curr_partition |= gate_to_qubit[n]
-        on_gate(n, gate_dict[n])
-        del S[idx]
-        for child in set(g[n]):
-            g[n].remove(child)
-            rg[child].remove(n)
-            if not rg[child]:
-                heapq.heappush(S, (tuple(sorted(gate_to_qubit[child])), child))
-    on_close()
-    total += len(parts[-1])
-    if total != len(gate_dict):
+        blocks[-1].append(item)
+        block_qubits |= dag.qubits[item]
+        for child in set(dag.succ[item]):
+            waiting[child] -= 1
+            if waiting[child] == 0:
+                ready.push(child)
+    if sum(len(b) for b in blocks) != len(dag.items):
         raise RuntimeError("partitioning lost gates")
-    return parts
+    return blocks
 
 
-def kahn_partition(c, max_qubit, preparts=None):
-    """Greedy Kahn partitioning of circuit c into partitions of at most max_qubit qubits.
-    Returns (partitioned circuit, parameter order [(source index, destination index,
-    count)], partitions [[gate index]])."""
-    parts = _kahn_walk(c, max_qubit, preparts, lambda n, gate: None, lambda: None)
-    return kahn_partition_preparts(c, max_qubit, preparts=parts)
+def _pieces(dag, blocks):
+    """Rule 5: every block split into its connected pieces, pieces in discovery order."""
+    out = []
+    for block in blocks:
+        left = set(block)
+        while left:
+            first = next(iter(left))
+            piece = {first}
+            left.remove(first)
+            frontier = [first]
+            while frontier:
+                node = frontier.pop()
+                for other in list(dag.pred[node]) + list(dag.succ[node]):
+                    if other in left:
+                        left.remove(other)
+                        piece.add(other)
+                        frontier.append(other)
+            out.append(piece)
+    return out
+
+
+def _assemble(circuit, dag, blocks):
+    """Sub-circuit per block and the parameter moves [(source start, destination start, count)]."""
+    n = circuit.get_Qbit_Num()
+    top = Circuit(n)
+    moves = []
+    dest = 0
+    for block in blocks:
+        sub = Circuit(n)
+        for item in block:
+            gate = dag.items[item]
+            sub.add_Gate(gate)
+            count = gate.get_Parameter_Num()
+            moves.append((gate.get_Parameter_Start_Index(), dest, count))
+            dest += count
+        top.add_Circuit(sub)
+    return top, moves
 
 
 def kahn_partition_preparts(c, max_qubit, preparts):
-    """The partitioned circuit of c for the predefined partitions preparts (each split into
-    its connected components first)."""
-    _, g, rg, _, _ = build_dependency(c)
-    preparts = split_partition(preparts, g, rg)
-    top = Circuit(c.get_Qbit_Num())
-    state = {"sub": Circuit(c.get_Qbit_Num()), "idx": 0}
-    param_order = []
-
-    def on_gate(n, gate):
-        state["sub"].add_Gate(gate)
-        param_order.append((gate.get_Parameter_Start_Index(), state["idx"], gate.get_Parameter_Num()))
-        state["idx"] += gate.get_Parameter_Num()
-
-    def on_close():
-        top.add_Circuit(state["sub"])
-        state["sub"] = Circuit(c.get_Qbit_Num())
-
-    parts = _kahn_walk(c, max_qubit, preparts, on_gate, on_close)
-    return top, param_order, parts
+    """Partitioned circuit of c whose blocks follow the given partitions (each split into its
+    connected pieces first).  Returns (partitioned circuit, parameter moves, blocks)."""
+    dag = _Dag(c)
+    pieces = _pieces(dag, preparts)
+    blocks = _greedy_blocks(dag, lambda k, _q, item: item in pieces[k])
+    top, moves = _assemble(c, dag, blocks)
+    return top, moves, blocks
 
 
-def split_partition(preparts, g, rg):
-    """Splits every partition into its connected components of the dependency graph, each
-    kept in the partition's order."""
-    L = []
-    for part in preparts:
-        V = set(part)
-        while V:
-            S = [next(iter(V))]
-            L.append(set())
-            while S:
-                node = S.pop()
-                if node not in V:
-                    continue
-                V.remove(node)
-                L[-1].add(node)
-                S.extend(rg[node])
-                S.extend(g[node])
-    ord_dict = {x: i for i, part in enumerate(preparts) for x in part}
-    return [list(sorted(x, key=ord_dict.get)) for x in L]
+def kahn_partition(c, max_qubit, preparts=None):
+    """Greedy partitioning of circuit c into blocks of at most max_qubit qubits.  Returns
+    (partitioned circuit, parameter moves [(source start, destination start, count)], blocks
+    [[item index]])."""
+    if preparts is None:
+        dag = _Dag(c)
+        preparts = _greedy_blocks(dag, lambda _k, q, item: len(q | dag.qubits[item]) <= max_qubit)
+    return kahn_partition_preparts(c, max_qubit, preparts)
 
 
 def translate_param_order(params, param_order):
     """Parameters of the original circuit rearranged for the partitioned circuit."""
-    params = np.asarray(params)
-    reordered = np.empty_like(params)
-    for s_idx, n_idx, n_params in param_order:
-        reordered[n_idx:n_idx + n_params] = params[s_idx:s_idx + n_params]
-    return reordered
+    src = np.asarray(params)
+    out = np.empty_like(src)
+    for start, dest, count in param_order:
+        out[dest:dest + count] = src[start:start + count]
+    return out
 
 
 def get_float_ops(num_qubit, gate_qubits, control_qubits, is_pure=False, io_penalty=48):
-    """FLOPs of applying a gate on gate_qubits qubits (control_qubits of them controls) to a
-    num_qubit state: 2^num_qubit amplitudes (2^(num_qubit - controls) for a pure controlled
-    gate), each a complex dot product of the gate's row (6 flops per complex multiply, 2 per
-    add) plus an io_penalty per amplitude."""
-    g_size = 2 ** (gate_qubits - control_qubits)
-    return 2 ** (num_qubit - (control_qubits if is_pure else 0)) * (g_size * (4 + 2) + 2 * (g_size - 1) + io_penalty)
+    """FLOP model of one gate application to a num_qubit register.  The gate acts as a dense
+    2^(gate_qubits - control_qubits) square block: each output amplitude is a row of that
+    block times the input, 6 flops per complex product and 2 per complex addition, plus
+    io_penalty for moving the amplitude.  A pure controlled gate touches only the
+    2^(num_qubit - control_qubits) amplitudes with its controls set; any other gate all
+    2^num_qubit."""
+    row = 1 << (gate_qubits - control_qubits)
+    per_amplitude = 8 * row - 2 + io_penalty
+    touched = 1 << (num_qubit - control_qubits) if is_pure else 1 << num_qubit
+    return touched * per_amplitude
 
 
 def parts_to_float_ops(num_qubit, gate_to_qubit, gate_to_tqubit, allparts):
-    """FLOPs of every partition applied as one fused gate on num_qubit qubits; with
-    gate_to_tqubit the non-target qubits count as controls, and a partition whose gates all
-    share one control set is a pure controlled gate."""
-    weights = []
+    """FLOP model of each block applied as one fused gate on num_qubit qubits.  With
+    gate_to_tqubit (item -> target qubit) the qubits that are no item's target count as
+    controls, and a block whose items all carry the same set of non-target qubits is a pure
+    controlled gate; without it every block is an uncontrolled dense gate."""
+    out = []
     for part in allparts:
-        qubits = set.union(*(gate_to_qubit[x] for x in part))
-        if gate_to_tqubit is not None:
-            tqubits = {gate_to_tqubit[x] for x in part}
-            is_pure = len({frozenset(gate_to_qubit[x] - {gate_to_tqubit[x]}) for x in part}) == 1
-            weights.append(get_float_ops(num_qubit, len(qubits), len(qubits) - len(tqubits), is_pure))
-        else:
-            weights.append(get_float_ops(num_qubit, len(qubits), 0, False))
-    return weights
+        used = set()
+        for item in part:
+            used |= gate_to_qubit[item]
+        if gate_to_tqubit is None:
+            out.append(get_float_ops(num_qubit, len(used), 0, False))
+            continue
+        targets = {gate_to_tqubit[item] for item in part}
+        others = {frozenset(gate_to_qubit[item] - {gate_to_tqubit[item]}) for item in part}
+        out.append(get_float_ops(num_qubit, len(used), len(used) - len(targets), len(others) == 1))
+    return out
 
 
 def total_float_ops(num_qubit, max_qubits_per_partition, gate_to_qubit, gate_to_tqubit, allparts):
-    """FLOPs of the whole partitioned circuit: the per-partition figures on
-    max_qubits_per_partition qubits scaled by 2^(num_qubit - max_qubits_per_partition)."""
-    weights = parts_to_float_ops(max_qubits_per_partition, gate_to_qubit, gate_to_tqubit, allparts)
-    return 2 ** (num_qubit - max_qubits_per_partition) * sum(weights)
+    """FLOP model of the whole partitioned circuit on num_qubit qubits: the blocks' figures on a
+    max_qubits_per_partition register, repeated for each of the 2^(num_qubit -
+    max_qubits_per_partition) sub-registers (a fraction when the register is smaller than a
+    block)."""
+    per_block = parts_to_float_ops(max_qubits_per_partition, gate_to_qubit, gate_to_tqubit, allparts)
+    spare = num_qubit - max_qubits_per_partition
+    return (1 << spare if spare >= 0 else 0.5 ** -spare) * sum(per_block)
 
 
 _UNAVAILABLE = {
