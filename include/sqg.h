@@ -112,15 +112,17 @@ size_t sqg_cost_grad_checkpoint_workspace_bytes(const sqg_circuit* circuit, int 
  * interface that hands over only the parameters, the cost and the gradient (there is no
  * place to pass a workspace and the callback runs thousands of times), or code whose
  * device memory belongs to a framework allocator that forbids raw cudaMalloc.  Same
- * arguments and results as sqg_cost_grad minus the workspace: the scratch is a 32 MiB
- * array compiled into the library, which every GPU that loads the library holds until the
- * process exits.  Requests needing more scratch than SQG_NOALLOC_SCRATCH_BYTES (see
- * sqg_cost_grad_workspace_bytes) fail with SQG_ERR_WORKSPACE.  The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress, with that device
- * current); make that first call before any stream capture.  All calls share the one
- * array, so calls that overlap on the GPU (other streams, other host threads) race; the
- * array keeps the last call's contents and every byte a call reads is written earlier in
- * the same call.  Allocates nothing. */
+ * arguments, checks and results as sqg_cost_grad minus the workspace: the scratch is a
+ * 32 MiB array compiled into the library, which every GPU that loads the library holds until
+ * the process exits.  Requests needing more scratch than SQG_NOALLOC_SCRATCH_BYTES (see
+ * sqg_cost_grad_workspace_bytes) fail with SQG_ERR_WORKSPACE; gradients up to five qubits
+ * without checkpoints need none.  The first call in each CUDA context (normally once per
+ * device) looks up the array's device address with cudaGetSymbolAddress in that context;
+ * make that first call before any stream capture (after a cudaDeviceReset the device has a
+ * new context and the next call does the set-up again).  All calls share the one array, so
+ * calls that overlap on the GPU (other streams, other host threads) race; the array keeps the
+ * last call's contents and every byte a call reads is written earlier in the same call.
+ * Allocates nothing. */
 int sqg_cost_grad_noalloc(const sqg_circuit* circuit, const double* theta_dev, int batch, const void* target_dev,
                           int cols, long long target_batch_stride, int trace_offset, int cost_variant,
                           double* cost_dev, double* grad_dev, int checkpoint_interval, void* stream);

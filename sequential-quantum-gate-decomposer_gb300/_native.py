@@ -23,6 +23,8 @@ NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", 
 
 # status codes and limits (sqg.h)
 SQG_OK = 0
+SQG_ERR_INVALID_ARGUMENT = 1
+SQG_ERR_UNSUPPORTED = 2
 SQG_ERR_WORKSPACE = 3
 SQG_NOALLOC_SCRATCH_BYTES = 32 << 20
 STATUS_TEXT = {0: "ok", 1: "invalid argument", 2: "unsupported configuration", 3: "workspace too small",

@@ -46,7 +46,9 @@ struct DecArgs {
   double tol;
   int max_calls, max_outer, loops, early_stop;
   unsigned long long seed;
-  double* zglob;
+  double* zglob;        // BFGS matrices in global memory: zslots slots of P * P doubles
+  unsigned int* zbits;  // occupancy bitmap of the slots (cleared before the launch)
+  int zslots;
   int z_in_smem;
   int cyclic;  // cost and gradient through the environment matrix (dec_eval_cyclic)
   int has_lam;  // 0: the one-chain environment form of a square target, which needs no lambda tiles
@@ -599,6 +601,43 @@ __device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
   return p;
 }
 
+// BFGS matrices in global memory are indexed by a slot that a CTA holds while it runs, not by
+// its target: there are only as many slots as CTAs of the launch can be resident at once, so
+// the matrices of a 4096-target launch stay within L2 instead of spreading over 4096 x 69 KB
+// and being written back to HBM.  A CTA claims the lowest free slot it finds (one atomicOr per
+// attempt on the occupancy bitmap) and clears its bit when it finishes; the bitmap is never
+// full when a CTA starts because fewer CTAs than slots are then resident.  Each scan is
+// bounded; after kClaimScans scans without a free slot the CTA gives up (-1).
+constexpr int kClaimScans = 1024;
+
+__device__ int claim_z_slot(unsigned int* bits, int slots) {
+  const int words = (slots + 31) / 32;
+  for (int scan = 0; scan < kClaimScans; ++scan) {
+    for (int w = 0; w < words; ++w) {
+      const unsigned int valid = (w == words - 1 && (slots & 31)) ? ((1u << (slots & 31)) - 1u) : 0xffffffffu;
+      unsigned int seen = *((volatile unsigned int*)&bits[w]);
+      // each pass either takes a bit or marks one more bit as taken: at most 32 passes
+      for (int pass = 0; pass < 32; ++pass) {
+        const unsigned int free_bits = ~seen & valid;
+        if (!free_bits) break;
+        const int bit = __ffs(free_bits) - 1;
+        const unsigned int old = atomicOr(&bits[w], 1u << bit);
+        if (!(old & (1u << bit))) {
+          __threadfence();
+          return w * 32 + bit;
+        }
+        seen = old | (1u << bit);
+      }
+    }
+  }
+  return -1;
+}
+
+__device__ void release_z_slot(unsigned int* bits, int slot) {
+  __threadfence();  // this CTA's writes to the slot are ordered before its release
+  atomicAnd(&bits[slot >> 5], ~(1u << (slot & 31)));
+}
+
 // Batched cost and gradient through the environment-matrix evaluation, one CTA per
 // parameter vector b (theta row b, target b * a.tstride; tstride 0 shares one target).
 template <int FORM>
@@ -634,8 +673,21 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     f0_vec = (double*)take(sizeof(double) * 100);
     dec_vec = (int*)take(sizeof(int) * 20);
     sh.Z = nullptr;
+  } else if (a.z_in_smem) {
+    sh.Z = (double*)take(sizeof(double) * P * P);
   } else {
-    sh.Z = a.z_in_smem ? (double*)take(sizeof(double) * P * P) : a.zglob + (long long)b * P * P;
+    __shared__ int z_slot;
+    if (threadIdx.x == 0) z_slot = claim_z_slot(a.zbits, a.zslots);
+    __syncthreads();
+    if (z_slot < 0) {  // no slot (not expected): report the instance as failed
+      if (threadIdx.x == 0) {
+        a.cost[b] = __longlong_as_double(0x7ff8000000000000LL);
+        a.calls[b] = -1;
+        if (a.iters) a.iters[b] = -1;
+      }
+      return;
+    }
+    sh.Z = a.zglob + (long long)z_slot * P * P;
   }
 
   for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = a.x[(long long)b * P + i];
@@ -689,6 +741,10 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     a.cost[b] = best;
     a.calls[b] = calls;
     if (a.iters) a.iters[b] = iters;
+  }
+  if (OPT == kBfgs && !a.z_in_smem) {
+    __syncthreads();  // every thread is done with Z
+    if (threadIdx.x == 0) release_z_slot(a.zbits, (int)((sh.Z - a.zglob) / ((long long)P * P)));
   }
 }
 
@@ -849,6 +905,51 @@ int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, v
   return dec_launch_form<OPT, kFormSweep>(c, a, batch, smem, stream);
 }
 
+template <int OPT, int FORM>
+int dec_max_active_per_sm(const sqg_circuit* c, size_t smem) {
+  int dev = 0, optin = 0, nb = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  if (smem > (size_t)optin) return 0;
+  if (cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_decompose<OPT, FORM>, dec_threads(c), smem) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+// Slots for the BFGS matrices of a launch of `batch` instances with Z in global memory: the
+// most CTAs of any evaluation form that the device can hold at once, at most one per
+// instance (one per instance if the occupancy cannot be queried).
+int dec_z_slots(const sqg_circuit* c, int cols, int batch) {
+  const size_t smem = dec_smem_bytes(c, cols, false);
+  int per_sm = std::max(dec_max_active_per_sm<kBfgs, kFormSweep>(c, smem),
+                        std::max(dec_max_active_per_sm<kBfgs, kFormCyclic>(c, smem),
+                                 dec_max_active_per_sm<kBfgs, kFormTwoChains>(c, smem)));
+  cudaGetLastError();  // a failed query leaves no error behind
+  int dev = 0, sms = 0;
+  if (per_sm <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+    return batch;
+  return (int)std::min<long long>(batch, (long long)per_sm * sms);
+}
+
+size_t round256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Bytes of the slot region: the matrices, then the occupancy bitmap.
+size_t dec_z_bytes(const sqg_circuit* c, int slots) {
+  return round256((size_t)slots * c->P * c->P * sizeof(double)) + round256((size_t)(slots + 31) / 32 * 4);
+}
+
+// Points a at the slot region at ws and clears its bitmap on the launch stream.
+int dec_use_z_slots(DecArgs& a, const sqg_circuit* c, int slots, void* ws, void* stream) {
+  a.zglob = (double*)ws;
+  a.zslots = slots;
+  a.zbits = (unsigned int*)((char*)ws + round256((size_t)slots * c->P * c->P * sizeof(double)));
+  cudaError_t e = cudaMemsetAsync(a.zbits, 0, (size_t)(slots + 31) / 32 * 4, (cudaStream_t)stream);
+  return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("slot bitmap: ") + cudaGetErrorString(e));
+}
+
 // Evaluation form of the decomposition kernels for this circuit and target width.
 void dec_eval_form(const sqg_circuit* c, int cols, int off, DecArgs& a) {
   a.has_lam = dec_needs_lam(c, cols) ? 1 : 0;
@@ -938,7 +1039,7 @@ extern "C" {
 size_t sqg_decompose_workspace_bytes(const sqg_circuit* c, int batch, int cols) {
   if (!c || batch <= 0 || cols <= 0) return 0;
   if (z_in_shared(c, cols)) return 256;
-  return (size_t)batch * c->P * c->P * sizeof(double) + 256;
+  return dec_z_bytes(c, dec_z_slots(c, cols, batch)) + 256;
 }
 
 int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, int batch, int trace_offset,
@@ -959,8 +1060,10 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   const bool zs = z_in_shared(c, cols);
   size_t smem = dec_smem_bytes(c, cols, zs);
   if (smem > 227 * 1024) return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
-  if (!zs && (!workspace || ws_bytes < (size_t)batch * c->P * c->P * sizeof(double)))
-    return set_error(SQG_ERR_WORKSPACE, "workspace too small for the per-instance BFGS matrices");
+  const int slots = zs ? 0 : dec_z_slots(c, cols, batch);
+  if (!zs && (!workspace || ((size_t)workspace & 255) || ws_bytes < dec_z_bytes(c, slots)))
+    return set_error(SQG_ERR_WORKSPACE, "workspace too small or not 256-byte aligned for the BFGS matrices: need " +
+                                            std::to_string(dec_z_bytes(c, slots)));
   DecArgs a = {};
   a.gates = c->d_gates;
   a.L = c->L; a.P = c->P; a.n = c->n; a.N = c->N; a.cols = cols;
@@ -974,8 +1077,9 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.max_calls = max_calls; a.max_outer = max_outer; a.loops = iteration_loops;
   a.early_stop = stop_at_tolerance;
   a.seed = seed;
-  a.zglob = (double*)workspace;
   a.z_in_smem = zs ? 1 : 0;
+  if (!zs)
+    if (int st = dec_use_z_slots(a, c, slots, workspace, stream)) return st;
   dec_eval_form(c, cols, off, a);
   return dec_launch<kBfgs>(c, a, batch, smem, stream);
 }
@@ -983,8 +1087,8 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
 
 size_t sqg_decompose_structures_workspace_bytes(const sqg_circuit* c, int batch, int cols) {
   if (!c || batch <= 0 || cols <= 0) return 0;
-  const size_t z = z_in_shared(c, cols) ? 0 : (size_t)batch * c->P * c->P * sizeof(double);
-  return (z + 255) / 256 * 256 + (size_t)batch * std::max(c->L, 1) * sizeof(Gate) + 256;
+  const size_t z = z_in_shared(c, cols) ? 0 : dec_z_bytes(c, dec_z_slots(c, cols, batch));
+  return z + (size_t)batch * std::max(c->L, 1) * sizeof(Gate) + 256;
 }
 
 int sqg_decompose_structures(const sqg_circuit* c, const sqg_gate* gates, const void* targets,
@@ -1012,7 +1116,8 @@ int sqg_decompose_structures(const sqg_circuit* c, const sqg_gate* gates, const 
   if (!workspace || ws_bytes < need || ((size_t)workspace & 255))
     return set_error(SQG_ERR_WORKSPACE, "workspace too small or not 256-byte aligned: need " + std::to_string(need));
   const int L = c->L, n = c->n;
-  const size_t zbytes = zs ? 0 : ((size_t)batch * c->P * c->P * sizeof(double) + 255) / 256 * 256;
+  const int slots = zs ? 0 : dec_z_slots(c, cols, batch);
+  const size_t zbytes = zs ? 0 : dec_z_bytes(c, slots);
   Gate* dgates = (Gate*)((char*)workspace + zbytes);
   if (int st = stage_gate_lists(c, gates, batch, dgates, stream)) return st;
   DecArgs a = {};
@@ -1029,8 +1134,9 @@ int sqg_decompose_structures(const sqg_circuit* c, const sqg_gate* gates, const 
   a.max_calls = max_calls; a.max_outer = max_outer; a.loops = iteration_loops;
   a.early_stop = stop_at_tolerance;
   a.seed = seed;
-  a.zglob = zs ? nullptr : (double*)workspace;
   a.z_in_smem = zs ? 1 : 0;
+  if (!zs)
+    if (int st = dec_use_z_slots(a, c, slots, workspace, stream)) return st;
   dec_eval_form(c, cols, off, a);
   return dec_launch<kBfgs>(c, a, batch, smem, stream);
 }

@@ -17,6 +17,7 @@
 //    instructions and everything else (index math, exchanges, sign flips) is integer work.
 //  * Deterministic reductions: per-tile partial traces go to the caller's workspace and
 //    are summed in a fixed order by a second kernel.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -621,9 +622,10 @@ size_t sqg_cost_grad_checkpoint_workspace_bytes(const sqg_circuit* c, int batch,
   return eval_layout(c, batch, cols, true, checkpoint_interval).end;
 }
 
-int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* target, int cols,
-                  long long target_batch_stride, int trace_offset, int variant, double* cost, double* grad,
-                  int checkpoint_interval, void* workspace, size_t ws_bytes, void* stream) {
+// Argument checks of sqg_cost_grad, shared with sqg_cost_grad_noalloc.
+static int cost_grad_args(const sqg_circuit* c, const double* theta, int B, const void* target, int cols,
+                          int trace_offset, int variant, const double* cost, const double* grad,
+                          int checkpoint_interval) {
   int st = check_circuit(c);
   if (st) return st;
   if (B <= 0 || B > 65535 || !target || !cost || cols <= 0)
@@ -637,6 +639,16 @@ int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* 
   const bool with_grad = grad != nullptr && c->P > 0;
   if (with_grad && c->n > 12) return fail(SQG_ERR_UNSUPPORTED, "gradient supports qbit_num <= 12");
   if (checkpoint_interval < 0) return fail(SQG_ERR_INVALID_ARGUMENT, "negative checkpoint interval");
+  return SQG_OK;
+}
+
+int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* target, int cols,
+                  long long target_batch_stride, int trace_offset, int variant, double* cost, double* grad,
+                  int checkpoint_interval, void* workspace, size_t ws_bytes, void* stream) {
+  int st = cost_grad_args(c, theta, B, target, cols, trace_offset, variant, cost, grad, checkpoint_interval);
+  if (st) return st;
+  const int off = variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
+  const bool with_grad = grad != nullptr && c->P > 0;
   if (with_grad && checkpoint_interval == 0) {
     // up to five qubits: one CTA per vector with the environment-matrix evaluation
     st = sqg::env_cost_grad(c, theta, B, target, cols, target_batch_stride, off, variant, cost, grad, stream);
@@ -688,29 +700,76 @@ int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* 
 }  // extern "C"
 
 // ---- allocation-free cost/gradient ---------------------------------------------------
-// The scratch of sqg_cost_grad_noalloc: a file-scope device array of fixed size.  Host
-// code must not take its address directly (that is a host-side stand-in); the device
-// address is looked up once per device with cudaGetSymbolAddress.
+// The scratch of sqg_cost_grad_noalloc: a file-scope device array of fixed size.  In host
+// code its name is a host-side stand-in, not a device address; the device address is looked
+// up with cudaGetSymbolAddress in the CUDA context that is current for the call, once per
+// context (a device normally has one, its primary context; a cudaDeviceReset or a driver-API
+// context made current gives the device another, and the array another address).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SQG_NOALLOC_SCRATCH_BYTES];
 
 namespace {
-constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoallocMaxDevices] = {};
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
 
-int noalloc_scratch(void** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
-  if (dev < 0 || dev >= kNoallocMaxDevices) return fail(SQG_ERR_UNSUPPORTED, "device ordinal beyond 63");
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(no-alloc scratch)");
-    g_noalloc_addr[dev] = p;
+struct NoallocSlot {
+  unsigned long long ctx_id;
+  void* addr;
+};
+constexpr int kNoallocSlots = 64;
+std::mutex g_noalloc_mu;
+NoallocSlot g_noalloc_slots[kNoallocSlots] = {};
+int g_noalloc_used = 0;
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+
+// Unique id of the current CUDA context (*have = false when none is current).  The two
+// driver functions are reached through the runtime's entry-point lookup, so the library
+// does not link the driver library itself.
+int current_context(unsigned long long* id, bool* have) {
+  if (!g_ctx_current || !g_ctx_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void**)&g_ctx_current, 12000,
+                                                      cudaEnableDefault, &q1);
+    cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&g_ctx_id, 12000, cudaEnableDefault, &q2);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !g_ctx_current || !g_ctx_id) {
+      g_ctx_current = nullptr;
+      g_ctx_id = nullptr;
+      return fail(SQG_ERR_CUDA, "cannot reach cuCtxGetCurrent/cuCtxGetId through the CUDA runtime");
+    }
   }
-  *out = g_noalloc_addr[dev];
+  CUcontext ctx = nullptr;
+  if (g_ctx_current(&ctx) != CUDA_SUCCESS) return fail(SQG_ERR_CUDA, "cuCtxGetCurrent failed");
+  *have = ctx != nullptr;
+  if (!ctx) return SQG_OK;
+  if (g_ctx_id(ctx, id) != CUDA_SUCCESS) return fail(SQG_ERR_CUDA, "cuCtxGetId failed");
+  return SQG_OK;
+}
+
+// Device address of the scratch array in the current context.
+int noalloc_scratch(void** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  unsigned long long id = 0;
+  bool have = false;
+  int st = current_context(&id, &have);
+  if (st) return st;
+  if (have) {
+    for (int i = 0; i < g_noalloc_used && i < kNoallocSlots; ++i)
+      if (g_noalloc_slots[i].ctx_id == id) {
+        *out = g_noalloc_slots[i].addr;
+        return SQG_OK;
+      }
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(no-alloc scratch)");
+  if (!have) {  // the runtime has just made its context current
+    if ((st = current_context(&id, &have))) return st;
+    if (!have) return fail(SQG_ERR_CUDA, "no CUDA context is current after cudaGetSymbolAddress");
+  }
+  g_noalloc_slots[g_noalloc_used % kNoallocSlots] = {id, p};
+  ++g_noalloc_used;
+  *out = p;
   return SQG_OK;
 }
 }  // namespace
@@ -720,11 +779,15 @@ extern "C" {
 int sqg_cost_grad_noalloc(const sqg_circuit* c, const double* theta, int B, const void* target, int cols,
                           long long target_batch_stride, int trace_offset, int variant, double* cost, double* grad,
                           int checkpoint_interval, void* stream) {
-  int st = check_circuit(c);
+  int st = cost_grad_args(c, theta, B, target, cols, trace_offset, variant, cost, grad, checkpoint_interval);
   if (st) return st;
-  if (B <= 0 || cols <= 0 || checkpoint_interval < 0)
-    return fail(SQG_ERR_INVALID_ARGUMENT, "bad batch, target width or checkpoint interval");
   const bool with_grad = grad != nullptr && c->P > 0;
+  if (with_grad && checkpoint_interval == 0) {
+    // up to five qubits the environment-matrix form takes no scratch at all
+    const int off = variant == SQG_FROBENIUS_NORM ? trace_offset : 0;
+    st = sqg::env_cost_grad(c, theta, B, target, cols, target_batch_stride, off, variant, cost, grad, stream);
+    if (st != SQG_ERR_UNSUPPORTED) return st;
+  }
   const size_t need = eval_layout(c, B, cols, with_grad, with_grad ? checkpoint_interval : 0).end;
   if (need > SQG_NOALLOC_SCRATCH_BYTES)
     return fail(SQG_ERR_WORKSPACE, "sqg_cost_grad_noalloc: this call needs " + std::to_string(need) +

@@ -132,16 +132,19 @@ class MLP:
         for i in range(L):
             fan_out, fan_in = self.W[i].shape
             last = i == L - 1
-            z = torch.empty((M, fan_out), dtype=torch.float32, device="cuda")
+            # inference needs the fp32 pre-activations of the output layer only
+            z = torch.empty((M, fan_out), dtype=torch.float32, device="cuda") if (keep or last) else None
             ab = None if last else torch.empty((M, fan_out), dtype=torch.bfloat16, device="cuda")
             # Z = A W^T + b; the next layer's input is ReLU(Z) in bf16
             if self.use_tc:
-                self._tc(a, self.Wb[i], M, fan_out, fan_in, C=z, bias=self.b[i])
+                if z is not None:
+                    self._tc(a, self.Wb[i], M, fan_out, fan_in, C=z, bias=self.b[i])
                 if not last:
                     self._tc(a, self.Wb[i], M, fan_out, fan_in, Cb=ab, bias=self.b[i], relu=True)
             else:
-                self._gemm(a, False, self.Wb[i], True, M, fan_out, fan_in, C=z, bias=self.b[i], lda=fan_in,
-                           ldb=fan_in)
+                if z is not None:
+                    self._gemm(a, False, self.Wb[i], True, M, fan_out, fan_in, C=z, bias=self.b[i], lda=fan_in,
+                               ldb=fan_in)
                 if not last:
                     self._gemm(a, False, self.Wb[i], True, M, fan_out, fan_in, Cb=ab, bias=self.b[i], relu=True,
                                lda=fan_in, ldb=fan_in)
