@@ -122,6 +122,29 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
     def _final_layer(self):
         return [(U3, q, -1) for q in range(self.qbit_num)]
 
+    # ---- gate structure built by the caller (wrapper methods of the reference class) -----
+    def _append_blocks(self, blocks):
+        for blk in blocks:
+            sub = Circuit(self.qbit_num)
+            for t, tg, c in blk:
+                sub._add(t, tg, c)
+            self.circuit.add_Circuit(sub)
+        self._evaluator = None
+
+    def add_Adaptive_Layers(self):
+        """add_adaptive_layers (N_Qubit_Decomposition_adaptive.cpp:1802-1820, wrapper
+        qgd_N_Qubit_Decompositions_Wrapper.cpp:2174): appends one level of adaptive layers,
+        a [U3(t), U3(c), CRY(t, c)] block per qubit pair, to the gate structure that the
+        Optimization_Problem family evaluates."""
+        self._append_blocks(self._adaptive_layer())
+        return 0
+
+    def add_Finalyzing_Layer_To_Gate_Structure(self):
+        """add_finalyzing_layer (N_Qubit_Decomposition_adaptive.cpp:1938-1968, wrapper :874):
+        appends a block of U3 gates on every qubit to the gate structure."""
+        self._append_blocks([self._final_layer()])
+        return 0
+
     # ---- inner decompositions (N_Qubit_Decomposition_custom runs) ---------------------------
     def _phase_target(self, factor):
         """apply_global_phase_factor on the decomposer's target."""

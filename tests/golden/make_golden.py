@@ -165,7 +165,40 @@ def config5():
           source_cost="reference", source_grad="oracle sweep")
 
 
-JOBS = {"umtx4": umtx4, "config1": config1, "config2": config2, "config3": config3, "config4": config4,
+def adaptive_n8_records(levels=2):
+    """8 qubits, `levels` levels of adaptive layers ([U3(t), U3(c), CRY(t, c)] for every pair
+    t < c) and the final U3 layer: the gate structure that add_Adaptive_Layers and
+    add_Finalyzing_Layer_To_Gate_Structure build."""
+    recs, p = [], 0
+    for _ in range(levels):
+        for t in range(8):
+            for c in range(t + 1, 8):
+                for g in ((7, t, -1), (7, c, -1), (14, t, c)):
+                    recs.append(g + (p,))
+                    p += 3 if g[0] == 7 else 1
+    for q in range(8):
+        recs.append((7, q, -1, p))
+        p += 3
+    return np.asarray(recs, dtype=np.int32), p
+
+
+def adaptive8():
+    """The reference's combined-optimisation check (tests/decomposition/
+    test_optmization_problem_combined.py): 8 qubits, two levels of adaptive layers, the target
+    cut to rows 80..239 with trace offset 80; cost and gradient at a second parameter set."""
+    recs, P = adaptive_n8_records()
+    rng = np.random.default_rng(880)
+    exact = rng.uniform(0, 2 * np.pi, P)
+    theta = rng.uniform(0, 2 * np.pi, (2, P))
+    U = R.get_matrix(8, recs, exact)
+    target = np.ascontiguousarray(U[80:240, :].conj().T)
+    c0, _ = R.cost_grad(8, recs, exact, target, trace_offset=80)
+    cg = [R.cost_grad(8, recs, th, target, trace_offset=80) for th in theta]
+    _save("adaptive_n8.npz", gates=recs, exact=exact, theta=theta, cost_exact=c0,
+          cost=np.array([a for a, _ in cg]), grad=np.stack([b for _, b in cg]), source="reference")
+
+
+JOBS = {"umtx4": umtx4, "adaptive8": adaptive8, "config1": config1, "config2": config2, "config3": config3, "config4": config4,
         "config5": config5}
 
 if __name__ == "__main__":
