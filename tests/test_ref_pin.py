@@ -191,3 +191,25 @@ def test_oracle_reproduces_the_reference_fixture_config5():
     _close(S @ Y, d["sketch"][0], 1e-11)
     cst = O.cost(12, d["gates"], theta[1], T, trace_offset=1000)
     assert cst == pytest.approx(d["cost"][1], abs=1e-14)
+
+
+def test_oracle_reproduces_the_reference_fixture_config3():
+    """10 qubits: the reference's costs (two of the 64 vectors) and the checksum of the target."""
+    from golden.inputs import config3_inputs
+
+    d = _load("config3_n10.npz")
+    c, angles, theta, pick = config3_inputs()
+    U = O.get_matrix(10, d["gates"], angles)
+    target = np.ascontiguousarray(U.conj().T)
+    assert np.max(np.abs(np.array([target.sum(), (target * target).sum()]) - d["target_checksum"])) < 1e-9
+    costs = O.batch(10, d["gates"], theta[:2], target)
+    _close(costs, d["cost"][:2], 1e-13)
+
+
+def test_oracle_reproduces_the_reference_fixture_adaptive8():
+    d = _load("adaptive_n8.npz")
+    U = O.get_matrix(8, d["gates"], d["exact"])
+    target = np.ascontiguousarray(U[80:240, :].conj().T)
+    c, g = O.cost_grad(8, d["gates"], d["theta"][0], target, trace_offset=80)
+    assert c == pytest.approx(float(d["cost"][0]), abs=1e-14)
+    _close(g, d["grad"][0], 1e-14)
