@@ -78,6 +78,26 @@ class BatchedDecomposer:
         return x, cost, calls
 
 
+    def run_sharded(self, targets_udag, x0, seed=0, group=None):
+        """run() across the ranks of a torch.distributed group (one process per GPU): each rank
+        decomposes its contiguous share of the batch, with the restart draws every instance
+        gets in the unsharded batch, and every rank receives the full results as host arrays
+        (x (B, P), cost (B,), calls (B,)).  The only exchange is the final gather, as in the
+        MPI_Allgather of optimization_problem_batched (Optimization_Interface.cpp:962-1006)."""
+        from . import sharding
+
+        T = np.asarray(targets_udag.cpu() if hasattr(targets_udag, "cpu") else targets_udag)
+        X = np.asarray(x0.cpu() if hasattr(x0, "cpu") else x0, dtype=np.float64)
+
+        def local(t, x, s):
+            if t.shape[0] == 0:
+                return np.zeros((0, X.shape[1])), np.zeros(0), np.zeros(0, dtype=np.int64)
+            xr, cr, nr = self.run(np.ascontiguousarray(t), np.ascontiguousarray(x), seed=s)
+            return xr.cpu().numpy(), cr.cpu().numpy(), nr.cpu().numpy().astype(np.int64)
+
+        return sharding.sharded_decompose(local, T, X, seed=seed, group=group)
+
+
 def adam_decompose_graph(circuit, target_udag, x0, tolerance=1e-8, max_iters=100000, eta=1e-3, adaptive_eta=True,
                          random_shift_count_max=100, randomization_threshold=2500000, max_outer=1,
                          current_minimum=None, seed=0, trace_offset=0, cost_variant=0, workspace=None, stream=None):

@@ -15,6 +15,7 @@ import numpy as np
 
 from . import _device as dev
 from . import _native
+from . import sharding
 from .circuit import Circuit, combined_unitary_device
 from .evaluator import FROBENIUS_NORM, SUPPORTED_VARIANTS, CostEvaluator
 from .batched import BatchedDecomposer, adam_decompose_graph, bfgs_decompose_graph
@@ -291,8 +292,19 @@ class N_Qubit_Decomposition_custom:
         p = np.ascontiguousarray(p, dtype=np.float64)
         if p.ndim != 2 or p.shape[1] != self.get_Parameter_Num():
             raise Exception("Optimization_Interface::optimization_problem: Wrong number of parameters.")
-        cost, _ = self.evaluator().cost_grad(dev.to_device_real(p), with_grad=False)
-        return cost.reshape(-1, 1).cpu().numpy()
+        def evaluate(rows):
+            if rows.shape[0] == 0:
+                return np.zeros(0), None
+            cost, _ = self.evaluator().cost_grad(dev.to_device_real(np.ascontiguousarray(rows)), with_grad=False)
+            return cost.cpu().numpy(), None
+
+        if sharding.distributed() is not None:
+            # one process per GPU: each rank evaluates its share, then all ranks gather (the
+            # reference's MPI path, Optimization_Interface.cpp:962-1006)
+            costs, _ = sharding.sharded_batch(evaluate, p)
+        else:
+            costs, _ = evaluate(p)
+        return np.asarray(costs).reshape(-1, 1)
 
     def Optimization_Problem_Combined_Unitary(self, parameters):
         p = self._params(parameters)
