@@ -287,26 +287,44 @@ def bench_ours(args, rank=0, world=1):
     seed0 = 1000 + 100000 * rank
 
     # learned initialiser: trained here, before any timed region, on decompositions the
-    # batched kernel generates (204800 synthetic targets, tcgen05 GEMMs)
-    init, train_stats = ini.train_initializer(ansatz, n_samples=204800, epochs=8, seed=4242)
+    # batched kernel generates (204800 synthetic targets, tcgen05 GEMMs).  --skip-learned
+    # (profiling runs only) reports the plain path alone.
+    if args.skip_learned:
+        init, train_stats = None, None
+    else:
+        init, train_stats = ini.train_initializer(ansatz, n_samples=204800, epochs=8, seed=4242)
     torch.cuda.synchronize()
 
     # plain path: random starts U[0, 2pi), generated on the host beforehand (part of the input)
     x0s = [torch.from_numpy(rng.uniform(0, 2 * np.pi, (N_TARGETS, P))).cuda() for _ in range(args.steps)]
     warm = [torch.from_numpy(rng.uniform(0, 2 * np.pi, (N_TARGETS, P))).cuda() for _ in range(args.warmup)]
     decomposition_steps(torch, decs, streams, flush, tdev, lambda k: warm[k], [seed0 + 50000 + k for k in range(args.warmup)])
-    decomposition_steps(torch, decs, streams, flush, tdev, lambda k: init.predict(tdev),
-                        [seed0 + 60000 + k for k in range(args.warmup)])
+    if init is not None:
+        decomposition_steps(torch, decs, streams, flush, tdev, lambda k: init.predict(tdev),
+                            [seed0 + 60000 + k for k in range(args.warmup)])
     clocks = Clocks()
     clocks.start()
     seeds = [seed0 + k for k in range(args.steps)]
     t_plain, res_plain = decomposition_steps(torch, decs, streams, flush, tdev, lambda k: x0s[k], seeds)
-    t_learn, res_learn = decomposition_steps(torch, decs, streams, flush, tdev, lambda k: init.predict(tdev), seeds)
+    if init is not None:
+        t_learn, res_learn = decomposition_steps(torch, decs, streams, flush, tdev, lambda k: init.predict(tdev),
+                                                 seeds)
     clk = clocks.stop()
-    init.mlp.check_errors()
     plain = path_stats(res_plain, t_plain, args.steps, P, flops_eval)
-    learned = path_stats(res_learn, t_learn, args.steps, P, flops_eval)
     plain["breakdown"] = breakdown(res_plain, P)
+    if init is None:
+        line = {"metric": METRIC, "value": plain["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": plain["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded Haar + random-circuit 3-qubit targets)",
+                "config": {"workload": "4096 3-qubit targets, 14-block NN ansatz, plain random-start path only "
+                                       "(profiling run)", "init": "random U[0,2pi)"},
+                "plain": plain, "gpu_launches": args.steps}
+        if clk:
+            line["clocks"] = clk
+        return line
+    init.mlp.check_errors()
+    learned = path_stats(res_learn, t_learn, args.steps, P, flops_eval)
     learned["breakdown"] = breakdown(res_learn, P)
 
     # end to end through host buffers (the same number of steps as the timed region)
@@ -432,6 +450,28 @@ def bench_gate_apply(sqg, wl, torch):
     res["fused"]["fp64_frac"] = res["fused"]["fp64_tflops"] / FP64_PEAK_TFLOPS
     res["unfused"]["hbm_frac"] = res["unfused"]["algorithmic_GBps"] / hbm
     res["unfused"]["fp64_tflops"] = 2.0 * B * fwd_ops / res["unfused"]["seconds"] / 1e12
+    # permutation/sign passes alone (CNOT and CZ, no FP64 instruction): one HBM pass per gate
+    crng = np.random.default_rng(55)
+    cc = sqg.Circuit(n)
+    for _ in range(200):
+        t_ = int(crng.integers(n))
+        ctl = int(crng.integers(n - 1))
+        ctl = ctl + 1 if ctl >= t_ else ctl
+        (cc.add_CNOT if crng.integers(2) == 0 else cc.add_CZ)(t_, ctl)
+    cbytes = sum(32.0 * N * N * frac[int(t)] for t, _, _, _ in cc.gate_records())
+    th0 = torch.zeros((B, 0), dtype=torch.float64, device="cuda")
+    cc.apply_to_device(th0, m, fused=False)
+    torch.cuda.synchronize()
+    e0.record()
+    cc.apply_to_device(th0, m, fused=False)
+    e1.record()
+    e1.synchronize()
+    tc = e0.elapsed_time(e1) / 1e3
+    res["unfused_cnot_cz_only"] = {"gates": 200, "seconds": tc, "algorithmic_GBps": B * cbytes / tc / 1e9,
+                                   "hbm_frac": B * cbytes / tc / 1e9 / hbm,
+                                   "note": "CNOT (exchange of the control=1 row pairs) and CZ (sign of a quarter "
+                                           "of the rows) passes execute no FP64 instruction: this is the HBM "
+                                           "bound of k_gate_hbm"}
     # one full cost + adjoint-gradient evaluation of the same circuit at n = 12
     ev = sqg.CostEvaluator(c, torch.eye(N, dtype=torch.complex128, device="cuda"))
     ev.cost_grad(th[:1])

@@ -887,12 +887,19 @@ int dec_launch_form(const sqg_circuit* c, const DecArgs& a, int batch, size_t sm
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (e == cudaSuccess && smem > (size_t)optin)
+  cudaFuncAttributes fa = {};
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_decompose<OPT, FORM>);
+  if (e == cudaSuccess && smem + fa.sharedSizeBytes > (size_t)optin)
     return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
-  // raised to the device maximum, never lowered: the attribute is shared by all callers
+  // raised to the device maximum (less the kernel's static shared memory), never lowered:
+  // the attribute is shared by all callers
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+    e = cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - (int)fa.sharedSizeBytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // leave no error behind for the next launch to report
+    return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  }
   k_decompose<OPT, FORM><<<batch, dec_threads(c), smem, (cudaStream_t)stream>>>(a);
   e = cudaGetLastError();
   return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
@@ -908,10 +915,13 @@ int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, v
 template <int OPT, int FORM>
 int dec_max_active_per_sm(const sqg_circuit* c, size_t smem) {
   int dev = 0, optin = 0, nb = 0;
+  cudaFuncAttributes fa = {};
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
-  if (smem > (size_t)optin) return 0;
-  if (cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess)
+  if (cudaFuncGetAttributes(&fa, k_decompose<OPT, FORM>) != cudaSuccess) return 0;
+  if (smem + fa.sharedSizeBytes > (size_t)optin) return 0;
+  if (cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           optin - (int)fa.sharedSizeBytes) != cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_decompose<OPT, FORM>, dec_threads(c), smem) != cudaSuccess)
     return 0;
