@@ -358,3 +358,25 @@ def test_small_register_cost_grad_forms_agree(sqg, monkeypatch, n, cols, offset,
     for cost, grad in ((ce, ge), (ct, gt)):
         assert np.allclose(cost.cpu().numpy(), cr, rtol=0, atol=1e-12)
         assert float(np.abs(grad.cpu().numpy() - gr).max()) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("n,cols", [(2, 4), (3, 8), (6, 12), (9, 64)])
+def test_unfused_cnot_cz_passes_match_oracle(sqg, n, cols):
+    """The HBM pass kernel of CNOT (row exchange) and CZ (sign flips of the target = 1 rows)
+    used by unfused application to matrices whose width is a multiple of 4."""
+    rng = np.random.default_rng(400 + n)
+    c = sqg.Circuit(n)
+    for _ in range(12):
+        t = int(rng.integers(n))
+        ctl = int(rng.integers(n - 1))
+        ctl = ctl + 1 if ctl >= t else ctl
+        (c.add_CNOT if rng.integers(2) == 0 else c.add_CZ)(t, ctl)
+    c.add_U3(0)
+    p = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    A = rng.standard_normal((1 << n, cols)) + 1j * rng.standard_normal((1 << n, cols))
+    dA = torch.from_numpy(np.stack([A, 2 * A])).cuda()
+    c.apply_to_device(torch.from_numpy(np.stack([p, p])).cuda(), dA, fused=False)
+    ref = O.get_matrix(n, c.gate_records(), p)
+    got = dA.cpu().numpy()
+    assert_close(got[0], ref @ A)
+    assert_close(got[1], ref @ (2 * A))
