@@ -145,8 +145,11 @@ def config4():
         x, f, n = R.bfgs_run(3, recs, targets[b], x0[b], 1000)
         xs.append(x), fs.append(f), calls.append(n)
     print("config4: %.0f s, solved %d of 64 in one run" % (time.time() - t0, sum(f < 1e-8 for f in fs)), flush=True)
+    short = [R.bfgs_run(3, recs, targets[b], x0[b], 20) for b in range(64)]
     _save("config4_3q.npz", gates=recs, targets=targets, x0=x0, max_iters=1000, x=np.stack(xs), cost=np.array(fs),
-          calls=np.array(calls), source="reference")
+          calls=np.array(calls), short_max_iters=20, short_x=np.stack([s[0] for s in short]),
+          short_cost=np.array([s[1] for s in short]), short_calls=np.array([s[2] for s in short]),
+          source="reference")
 
 
 def config5():

@@ -37,8 +37,9 @@ def test_learned_initializer_gain_over_random_start(sqg):
     per_r = calls_r.double().sum().item() / max(ok_r, 1)
     print("learned: solved %d, evaluations per solved target %.1f; random: solved %d, %.1f" % (ok_l, per_l, ok_r,
                                                                                                  per_r))
-    # every result is certified by the FP64 cost; the learned start must not cost more
-    # evaluations per successful decomposition than the random start (measured gain on the
-    # full 4096-target workload: about 7 %)
-    assert ok_l >= 0.9 * ok_r
-    assert per_l <= 1.05 * per_r
+    # every result is certified by the FP64 cost; the learned start must save evaluations per
+    # successful decomposition (a strict gain; on the full 4096-target benchmark workload the
+    # gain is about 6 %, far from the 3x target, for the measured reason that the network's
+    # starts are not within the BFGS basin) while solving as many targets within 1 %
+    assert ok_l >= ok_r - 10, (ok_l, ok_r)
+    assert per_l < per_r, (per_l, per_r)
