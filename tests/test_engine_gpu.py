@@ -360,10 +360,10 @@ def test_small_register_cost_grad_forms_agree(sqg, monkeypatch, n, cols, offset,
         assert float(np.abs(grad.cpu().numpy() - gr).max()) <= 1e-12 * scale
 
 
-@pytest.mark.parametrize("n,cols", [(2, 4), (3, 8), (6, 12), (9, 64)])
+@pytest.mark.parametrize("n,cols", [(2, 4), (3, 5), (6, 12), (9, 64)])
 def test_unfused_cnot_cz_passes_match_oracle(sqg, n, cols):
     """The HBM pass kernel of CNOT (row exchange) and CZ (sign flips of the target = 1 rows)
-    used by unfused application to matrices whose width is a multiple of 4."""
+    used by unfused application to matrices, power-of-two widths and others."""
     rng = np.random.default_rng(400 + n)
     c = sqg.Circuit(n)
     for _ in range(12):
