@@ -49,7 +49,6 @@ struct DecArgs {
   double* zglob;        // BFGS matrices in global memory: zslots slots of P * P doubles
   unsigned int* zbits;  // occupancy bitmap of the slots (cleared before the launch)
   int zslots;
-  int zgroup;  // > 0: SM s owns slots [s * zgroup, (s + 1) * zgroup); 0: one shared pool
   int z_in_smem;
   int cyclic;  // cost and gradient through the environment matrix (dec_eval_cyclic)
   int has_lam;  // 0: the one-chain environment form of a square target, which needs no lambda tiles
@@ -605,58 +604,29 @@ __device__ char* dec_setup(const DecArgs& a, Sh& sh, int b, char* p) {
 // BFGS matrices in global memory are indexed by a slot that a CTA holds while it runs, not by
 // its target: there are only as many slots as CTAs of the launch can be resident at once, so
 // the matrices of a 4096-target launch stay within L2 instead of spreading over 4096 x 69 KB
-// and being written back to HBM.  For large launches each SM owns a group of slots (as many as
-// it can hold CTAs, rounded up to a power of two), so the matrices an SM touches stay in the
-// same region: the L2 partition next to an SM caches what that SM accesses, and the matrices of
-// one die's SMs then fit in its partition.  A CTA claims the lowest free slot of its SM's group
-// (one atomicOr per attempt on the occupancy bitmap), or, if that group is full or the launch
-// uses one shared pool, the lowest free slot anywhere, and clears its bit when it finishes; the
-// bitmap is never full when a CTA starts because fewer CTAs than slots are then resident.  Each
-// scan is bounded; after kClaimScans scans without a free slot the CTA gives up (-1).
+// and being written back to HBM.  A CTA claims the lowest free slot it finds (one atomicOr per
+// attempt on the occupancy bitmap) and clears its bit when it finishes; the bitmap is never
+// full when a CTA starts because fewer CTAs than slots are then resident.  Each scan is
+// bounded; after kClaimScans scans without a free slot the CTA gives up (-1).
 constexpr int kClaimScans = 1024;
 
-__device__ __forceinline__ unsigned int sm_id() {
-  unsigned int r;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
-  return r;
-}
-
-// Lowest free bit of bits[w] within mask, taken with atomicOr; -1 when none is free.  Each
-// pass either takes a bit or marks one more bit as taken: at most 32 passes.
-__device__ int claim_bit(unsigned int* bits, int w, unsigned int mask) {
-  unsigned int seen = *((volatile unsigned int*)&bits[w]);
-  for (int pass = 0; pass < 32; ++pass) {
-    const unsigned int free_bits = ~seen & mask;
-    if (!free_bits) return -1;
-    const int bit = __ffs(free_bits) - 1;
-    const unsigned int old = atomicOr(&bits[w], 1u << bit);
-    if (!(old & (1u << bit))) return w * 32 + bit;
-    seen = old | (1u << bit);
-  }
-  return -1;
-}
-
-__device__ int claim_z_slot(unsigned int* bits, int slots, int group) {
-  if (group > 0) {
-    const unsigned int sm = sm_id();
-    if ((long long)(sm + 1) * group <= slots) {
-      const int first = (int)sm * group;
-      const unsigned int mask = (group >= 32 ? 0xffffffffu : ((1u << group) - 1u)) << (first & 31);
-      const int got = claim_bit(bits, first >> 5, mask);
-      if (got >= 0) {
-        __threadfence();
-        return got;
-      }
-    }
-  }
+__device__ int claim_z_slot(unsigned int* bits, int slots) {
   const int words = (slots + 31) / 32;
   for (int scan = 0; scan < kClaimScans; ++scan) {
     for (int w = 0; w < words; ++w) {
       const unsigned int valid = (w == words - 1 && (slots & 31)) ? ((1u << (slots & 31)) - 1u) : 0xffffffffu;
-      const int got = claim_bit(bits, w, valid);
-      if (got >= 0) {
-        __threadfence();
-        return got;
+      unsigned int seen = *((volatile unsigned int*)&bits[w]);
+      // each pass either takes a bit or marks one more bit as taken: at most 32 passes
+      for (int pass = 0; pass < 32; ++pass) {
+        const unsigned int free_bits = ~seen & valid;
+        if (!free_bits) break;
+        const int bit = __ffs(free_bits) - 1;
+        const unsigned int old = atomicOr(&bits[w], 1u << bit);
+        if (!(old & (1u << bit))) {
+          __threadfence();
+          return w * 32 + bit;
+        }
+        seen = old | (1u << bit);
       }
     }
   }
@@ -707,7 +677,7 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     sh.Z = (double*)take(sizeof(double) * P * P);
   } else {
     __shared__ int z_slot;
-    if (threadIdx.x == 0) z_slot = claim_z_slot(a.zbits, a.zslots, a.zgroup);
+    if (threadIdx.x == 0) z_slot = claim_z_slot(a.zbits, a.zslots);
     __syncthreads();
     if (z_slot < 0) {  // no slot (not expected): report the instance as failed
       if (threadIdx.x == 0) {
@@ -958,16 +928,10 @@ int dec_max_active_per_sm(const sqg_circuit* c, size_t smem) {
   return nb;
 }
 
-// Slots for the BFGS matrices of a launch of `batch` instances with Z in global memory.  A
-// launch that fills the device gets a group of slots per SM (the most CTAs of any evaluation
-// form an SM can hold, rounded up to a power of two: groups never straddle a bitmap word); a
-// smaller launch gets one shared pool with one slot per instance.  One slot per instance, in a
-// shared pool, if the occupancy cannot be queried.
-struct ZLayout {
-  int slots, group;
-};
-
-ZLayout dec_z_layout(const sqg_circuit* c, int cols, int batch) {
+// Slots for the BFGS matrices of a launch of `batch` instances with Z in global memory: the
+// most CTAs of any evaluation form that the device can hold at once, at most one per
+// instance (one per instance if the occupancy cannot be queried).
+int dec_z_slots(const sqg_circuit* c, int cols, int batch) {
   const size_t smem = dec_smem_bytes(c, cols, false);
   int per_sm = std::max(dec_max_active_per_sm<kBfgs, kFormSweep>(c, smem),
                         std::max(dec_max_active_per_sm<kBfgs, kFormCyclic>(c, smem),
@@ -976,16 +940,9 @@ ZLayout dec_z_layout(const sqg_circuit* c, int cols, int batch) {
   int dev = 0, sms = 0;
   if (per_sm <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-    return {batch, 0};
-  const long long resident = (long long)per_sm * sms;
-  if (batch < resident) return {batch, 0};
-  int group = 1;
-  while (group < per_sm) group <<= 1;
-  if (group > 32) return {(int)std::min<long long>(batch, resident), 0};
-  return {sms * group, group};
+    return batch;
+  return (int)std::min<long long>(batch, (long long)per_sm * sms);
 }
-
-int dec_z_slots(const sqg_circuit* c, int cols, int batch) { return dec_z_layout(c, cols, batch).slots; }
 
 size_t round256(size_t x) { return (x + 255) / 256 * 256; }
 
@@ -995,11 +952,9 @@ size_t dec_z_bytes(const sqg_circuit* c, int slots) {
 }
 
 // Points a at the slot region at ws and clears its bitmap on the launch stream.
-int dec_use_z_slots(DecArgs& a, const sqg_circuit* c, int cols, int batch, int slots, void* ws, void* stream) {
+int dec_use_z_slots(DecArgs& a, const sqg_circuit* c, int slots, void* ws, void* stream) {
   a.zglob = (double*)ws;
   a.zslots = slots;
-  const ZLayout zl = dec_z_layout(c, cols, batch);
-  a.zgroup = zl.slots == slots ? zl.group : 0;
   a.zbits = (unsigned int*)((char*)ws + round256((size_t)slots * c->P * c->P * sizeof(double)));
   cudaError_t e = cudaMemsetAsync(a.zbits, 0, (size_t)(slots + 31) / 32 * 4, (cudaStream_t)stream);
   return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("slot bitmap: ") + cudaGetErrorString(e));
@@ -1134,7 +1089,7 @@ int sqg_decompose_batched(const sqg_circuit* c, const void* targets, int cols, i
   a.seed = seed;
   a.z_in_smem = zs ? 1 : 0;
   if (!zs)
-    if (int st = dec_use_z_slots(a, c, cols, batch, slots, workspace, stream)) return st;
+    if (int st = dec_use_z_slots(a, c, slots, workspace, stream)) return st;
   dec_eval_form(c, cols, off, a);
   return dec_launch<kBfgs>(c, a, batch, smem, stream);
 }
@@ -1191,7 +1146,7 @@ int sqg_decompose_structures(const sqg_circuit* c, const sqg_gate* gates, const 
   a.seed = seed;
   a.z_in_smem = zs ? 1 : 0;
   if (!zs)
-    if (int st = dec_use_z_slots(a, c, cols, batch, slots, workspace, stream)) return st;
+    if (int st = dec_use_z_slots(a, c, slots, workspace, stream)) return st;
   dec_eval_form(c, cols, off, a);
   return dec_launch<kBfgs>(c, a, batch, smem, stream);
 }
