@@ -343,14 +343,87 @@ int set_smem(K kernel, size_t bytes) {
 }
 
 struct PrepLayout {
-  size_t gm_off, sc_off, end;
+  size_t gm_off, sc_off, mg_off, end;
 };
 PrepLayout prep_layout(const sqg_circuit* c, int B, size_t start) {
   PrepLayout l;
   l.gm_off = align_up(start, 256);
   l.sc_off = align_up(l.gm_off + (size_t)B * std::max(c->L, 1) * sizeof(GateMat), 256);
-  l.end = align_up(l.sc_off + (size_t)B * std::max(c->P, 1) * sizeof(double2), 256);
+  l.mg_off = align_up(l.sc_off + (size_t)B * std::max(c->P, 1) * sizeof(double2), 256);
+  l.end = align_up(l.mg_off + (size_t)B * c->Lm * sizeof(GateMat), 256);
   return l;
+}
+
+// Full 2x2 matrix of a single-qubit gate from its GateMat (k_prep's storage: U3 whole, the
+// one-parameter gates as (cos, sin) in u[0]).
+__device__ __forceinline__ void full_matrix(int type, const GateMat& m, double2 u[4]) {
+  const double c = m.u[0].x, s = m.u[0].y;
+  if (type == G_U3) {
+    u[0] = m.u[0]; u[1] = m.u[1]; u[2] = m.u[2]; u[3] = m.u[3];
+  } else if (type == G_RY) {
+    u[0] = make_double2(c, 0.0); u[1] = make_double2(dneg(s), 0.0);
+    u[2] = make_double2(s, 0.0); u[3] = make_double2(c, 0.0);
+  } else if (type == G_RX) {
+    u[0] = make_double2(c, 0.0); u[1] = make_double2(0.0, dneg(s));
+    u[2] = make_double2(0.0, dneg(s)); u[3] = make_double2(c, 0.0);
+  } else {  // G_RZ
+    u[0] = make_double2(c, dneg(s)); u[1] = make_double2(0.0, 0.0);
+    u[2] = make_double2(0.0, 0.0); u[3] = make_double2(c, s);
+  }
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+// Gate matrices of the merged forward plan, one thread per (instance, merged gate): a kept
+// gate copies its matrix, a merged run multiplies its members' matrices in circuit order
+// (M = G_k ... G_1).
+__global__ void k_merge(const Gate* __restrict__ gates, const GateMat* __restrict__ gm, int L,
+                        const Gate* __restrict__ mgates, const int* __restrict__ mfirst,
+                        const int* __restrict__ members, int Lm, GateMat* __restrict__ out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (m >= Lm) return;
+  const GateMat* g = gm + (long long)b * L;
+  const int f = mfirst[m], e = mfirst[m + 1];
+  GateMat r;
+  if (mgates[m].type != G_GEN) {
+    r = g[members[f]];
+  } else {
+    double2 M[4];
+    full_matrix(gates[members[f]].type, g[members[f]], M);
+    for (int k = f + 1; k < e; k++) {
+      double2 G[4], R[4];
+      full_matrix(gates[members[k]].type, g[members[k]], G);
+      R[0] = cmul(G[0], M[0]); R[0].x += cmul(G[1], M[2]).x; R[0].y += cmul(G[1], M[2]).y;
+      R[1] = cmul(G[0], M[1]); R[1].x += cmul(G[1], M[3]).x; R[1].y += cmul(G[1], M[3]).y;
+      R[2] = cmul(G[2], M[0]); R[2].x += cmul(G[3], M[2]).x; R[2].y += cmul(G[3], M[2]).y;
+      R[3] = cmul(G[2], M[1]); R[3].x += cmul(G[3], M[3]).x; R[3].y += cmul(G[3], M[3]).y;
+      M[0] = R[0]; M[1] = R[1]; M[2] = R[2]; M[3] = R[3];
+    }
+    r.u[0] = M[0]; r.u[1] = M[1]; r.u[2] = M[2]; r.u[3] = M[3];
+  }
+  out[(long long)b * Lm + m] = r;
+}
+
+// Forward gate list and matrices of a tile launch: the merged plan when the circuit has one
+// (its matrices computed into the workspace at prep.mg_off), else the gates themselves.
+int forward_plan(const sqg_circuit* c, const PrepLayout& prep, char* ws, int B, const GateMat* gm, TileArgs& a,
+                 cudaStream_t st) {
+  if (c->Lm == 0) {
+    a.gates = c->d_gates;
+    a.L = c->L;
+    a.gm = gm;
+    return SQG_OK;
+  }
+  GateMat* mg = (GateMat*)(ws + prep.mg_off);
+  k_merge<<<dim3((c->Lm + 127) / 128, B), 128, 0, st>>>(c->d_gates, gm, c->L, c->d_mgates, c->d_mfirst,
+                                                         c->d_mmembers, c->Lm, mg);
+  a.gates = c->d_mgates;
+  a.L = c->Lm;
+  a.gm = mg;
+  return cuda_status(cudaGetLastError(), "k_merge");
 }
 
 struct EvalLayout {
@@ -555,6 +628,60 @@ __global__ void __launch_bounds__(kStateThreads) k_state_block(StateArgs a) {
 // =====================================================================================
 // C ABI
 // =====================================================================================
+// Merged forward plan: walking the gates in order, single-qubit gates collect per qubit; a
+// two-qubit gate first emits the open runs of its two qubits, then itself; the remaining runs
+// are emitted at the end.  This only moves single-qubit gates past gates on other qubits, with
+// which they commute.  A run becomes one general 2x2 gate (16 FP64 instructions per amplitude
+// pair) when its members cost more (U3 14, RX/RY/RZ 8), otherwise its members stay.  The plan is
+// kept only if it removes work; the adjoint and right-application paths use the gates as given.
+int build_merge_plan(sqg_circuit* c) {
+  const std::vector<Gate>& g = c->h_gates;
+  std::vector<std::vector<int>> open(c->n);
+  std::vector<Gate> mg;
+  std::vector<int> first{0}, members;
+  bool merged = false;
+  auto cost1 = [](int type) { return type == G_U3 ? 14 : 8; };
+  auto emit_one = [&](int i) {
+    mg.push_back(g[i]);
+    members.push_back(i);
+    first.push_back((int)members.size());
+  };
+  auto flush = [&](int q) {
+    std::vector<int>& run = open[q];
+    int sum = 0;
+    for (int i : run) sum += cost1(g[i].type);
+    if (run.size() >= 2 && sum > 16) {
+      mg.push_back(Gate{G_GEN, q, -1, -1});
+      members.insert(members.end(), run.begin(), run.end());
+      first.push_back((int)members.size());
+      merged = true;
+    } else {
+      for (int i : run) emit_one(i);
+    }
+    run.clear();
+  };
+  for (int i = 0; i < c->L; i++) {
+    if (gate_controlled(g[i].type)) {
+      flush(g[i].target);
+      flush(g[i].control);
+      emit_one(i);
+    } else {
+      open[g[i].target].push_back(i);
+    }
+  }
+  for (int q = 0; q < c->n; q++) flush(q);
+  if (!merged) return SQG_OK;
+  c->Lm = (int)mg.size();
+  cudaError_t e = cudaMalloc(&c->d_mgates, sizeof(Gate) * mg.size());
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_mfirst, sizeof(int) * first.size());
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_mmembers, sizeof(int) * members.size());
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_mgates, mg.data(), sizeof(Gate) * mg.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_mfirst, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->d_mmembers, members.data(), sizeof(int) * members.size(), cudaMemcpyHostToDevice);
+  return cuda_status(e, "merged forward plan");
+}
+
 extern "C" {
 
 const char* sqg_status_string(int status) {
@@ -621,6 +748,7 @@ int sqg_circuit_create(int qbit_num, const sqg_gate* gates, int gate_num, sqg_ci
     }
   }
   int st = build_state_plan(c);
+  if (!st) st = build_merge_plan(c);
   if (st) {
     sqg_circuit_destroy(c);
     return st;
@@ -656,6 +784,9 @@ int sqg_circuit_destroy(sqg_circuit* c) {
   if (c->d_lgates) cudaFree(c->d_lgates);
   if (c->d_hitab) cudaFree(c->d_hitab);
   if (c->d_inact) cudaFree(c->d_inact);
+  if (c->d_mgates) cudaFree(c->d_mgates);
+  if (c->d_mfirst) cudaFree(c->d_mfirst);
+  if (c->d_mmembers) cudaFree(c->d_mmembers);
   delete c;
   return SQG_OK;
 }
@@ -740,6 +871,7 @@ int sqg_cost_grad(const sqg_circuit* c, const double* theta, int B, const void* 
     if ((st = set_smem(k_tile_adjoint, l.plan.smem))) return st;
     k_tile_adjoint<<<grid, l.plan.threads, l.plan.smem, s>>>(a);
   } else {
+    if ((st = forward_plan(c, l.prep, ws, B, gm, a, s))) return st;
     if ((st = set_smem(k_tile_forward<false, true>, l.plan.smem))) return st;
     k_tile_forward<false, true><<<grid, l.plan.threads, l.plan.smem, s>>>(a);
   }
@@ -887,6 +1019,7 @@ int sqg_apply(const sqg_circuit* c, const double* theta, int B, void* mtx, int c
     a.TC = pl.TC;
     a.tiles = pl.tiles;
     a.orient = ORIENT_FWD;
+    if ((st = forward_plan(c, l, ws, B, gm, a, s))) return st;
     if ((st = set_smem(k_tile_forward<true, false>, pl.smem))) return st;
     k_tile_forward<true, false><<<dim3(pl.tiles, B), pl.threads, pl.smem, s>>>(a);
     return cuda_status(cudaGetLastError(), "k_tile_forward");

@@ -14,6 +14,10 @@ namespace sqg {
 
 // Gate type ids of SQUANDER (src-cpp/gates/include/Gate.h:37-50).
 enum : int { G_CZ = 4, G_CNOT = 5, G_U3 = 7, G_RY = 8, G_RX = 9, G_RZ = 10, G_CRY = 14 };
+// Internal only (never in a caller's gate list): a general 2x2 unitary on one qubit, the product
+// of a run of single-qubit gates in the merged forward plan (the id of SQUANDER's
+// GENERAL_OPERATION).
+enum : int { G_GEN = 1 };
 
 struct Gate {
   int type, target, control, pstart;
@@ -62,6 +66,17 @@ __device__ __forceinline__ void rule_u3(double2& x, double2& y, double u00, doub
   x = nx;
   y = ny;
 }
+// General 2x2 [[u00, u01], [u10, u11]] with u00 = a + i s: 16 FP64 instructions.
+__device__ __forceinline__ void rule_gen(double2& x, double2& y, double a, double s, double2 u01, double2 u10,
+                                         double2 u11) {
+  double2 nx, ny;
+  nx.x = fma(a, x.x, fma(-s, x.y, fma(u01.x, y.x, -u01.y * y.y)));
+  nx.y = fma(a, x.y, fma(s, x.x, fma(u01.x, y.y, u01.y * y.x)));
+  ny.x = fma(u10.x, x.x, fma(-u10.y, x.y, fma(u11.x, y.x, -u11.y * y.y)));
+  ny.y = fma(u10.x, x.y, fma(u10.y, x.x, fma(u11.x, y.y, u11.y * y.x)));
+  x = nx;
+  y = ny;
+}
 // RY / CRY [[c, -s], [s, c]]: 8 FP64 instructions.
 __device__ __forceinline__ void rule_ry(double2& x, double2& y, double c, double s) {
   double2 nx, ny;
@@ -97,7 +112,7 @@ __device__ __forceinline__ void rule_rz(double2& x, double2& y, double c, double
 // transposed (G^T: right multiplication by G) or conjugated (conj G = (G^dagger)^T: right
 // multiplication by G^dagger) update.
 struct PairOp {
-  int kind;  // G_U3, G_RY (also CRY), G_RX, G_RZ, G_CNOT, G_CZ
+  int kind;  // G_U3, G_RY (also CRY), G_RX, G_RZ, G_CNOT, G_CZ, G_GEN
   double a;  // u00 (U3) or cos
   double s;  // sin (signed for adjoint)
   double2 b, c, d;  // u01, u10, u11 (U3)
@@ -129,6 +144,22 @@ __device__ __forceinline__ PairOp make_op(int type, const GateMat& m, int orient
       op.c = make_double2(m.u[2].x, dneg(m.u[2].y));
       op.d = make_double2(m.u[3].x, dneg(m.u[3].y));
     }
+  } else if (type == G_GEN) {
+    // u00 = a + i s (op.a, op.s), u01 = b, u10 = c, u11 = d as stored
+    if (orient == ORIENT_ADJ) {  // [[conj u00, conj u10], [conj u01, conj u11]]
+      op.s = dneg(op.s);
+      op.b = make_double2(m.u[2].x, dneg(m.u[2].y));
+      op.c = make_double2(m.u[1].x, dneg(m.u[1].y));
+      op.d = make_double2(m.u[3].x, dneg(m.u[3].y));
+    } else if (orient == ORIENT_TRANS) {
+      op.b = m.u[2];
+      op.c = m.u[1];
+    } else if (orient == ORIENT_CONJ) {
+      op.s = dneg(op.s);
+      op.b = make_double2(m.u[1].x, dneg(m.u[1].y));
+      op.c = make_double2(m.u[2].x, dneg(m.u[2].y));
+      op.d = make_double2(m.u[3].x, dneg(m.u[3].y));
+    }
   } else if (type == G_RY || type == G_CRY) {
     // RY^dagger = RY^T = RY(-theta); RY is real, so conj RY = RY
     if (orient == ORIENT_ADJ || orient == ORIENT_TRANS) op.s = dneg(op.s);
@@ -142,6 +173,7 @@ __device__ __forceinline__ PairOp make_op(int type, const GateMat& m, int orient
 __device__ __forceinline__ void apply_op(const PairOp& op, double2& x, double2& y) {
   switch (op.kind) {
     case G_U3: rule_u3(x, y, op.a, op.b, op.c, op.d); break;
+    case G_GEN: rule_gen(x, y, op.a, op.s, op.b, op.c, op.d); break;
     case G_RY: rule_ry(x, y, op.a, op.s); break;
     case G_RX: rule_rx(x, y, op.a, op.s); break;
     case G_RZ: rule_rz(x, y, op.a, op.s); break;

@@ -25,6 +25,13 @@ struct sqg_circuit {
   sqg::Gate* d_lgates = nullptr;
   int* d_hitab = nullptr;
   int* d_inact = nullptr;
+  // merged forward plan (Lm > 0 when it saves work): runs of single-qubit gates on one qubit
+  // with no two-qubit gate on that qubit between them become one general 2x2 gate; d_mgates
+  // holds the Lm records, members d_mmembers[d_mfirst[m] .. d_mfirst[m + 1]) their source gates
+  int Lm = 0;
+  sqg::Gate* d_mgates = nullptr;
+  int* d_mfirst = nullptr;
+  int* d_mmembers = nullptr;
 };
 
 namespace sqg {

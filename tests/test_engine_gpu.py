@@ -380,3 +380,36 @@ def test_unfused_cnot_cz_passes_match_oracle(sqg, n, cols):
     got = dA.cpu().numpy()
     assert_close(got[0], ref @ A)
     assert_close(got[1], ref @ (2 * A))
+
+
+@pytest.mark.parametrize("n", [1, 3, 7, 12])
+def test_merged_single_qubit_runs_match_oracle(sqg, n):
+    """Runs of single-qubit gates (U3, RX, RY, RZ) with no two-qubit gate on their qubit between
+    them are applied as one general 2x2 gate by the fused forward paths (application and
+    cost-only evaluation); their results equal the oracle's gate-by-gate ones."""
+    rng = np.random.default_rng(500 + n)
+    c = sqg.Circuit(n)
+    for _ in range(40):
+        t = int(rng.integers(n))
+        for _ in range(int(rng.integers(1, 5))):
+            getattr(c, "add_" + ("U3", "RX", "RY", "RZ")[int(rng.integers(4))])(t)
+        if n > 1 and rng.integers(2):
+            ctl = int(rng.integers(n - 1))
+            ctl = ctl + 1 if ctl >= t else ctl
+            getattr(c, "add_" + ("CNOT", "CZ", "CRY")[int(rng.integers(3))])(t, ctl)
+    P = c.get_Parameter_Num()
+    recs = c.gate_records()
+    p = rng.uniform(0, 2 * np.pi, (2, P))
+    N = 1 << n
+    cols = min(N, 16)
+    A = rng.standard_normal((N, cols)) + 1j * rng.standard_normal((N, cols))
+    dA = torch.from_numpy(np.stack([A, A])).cuda()
+    c.apply_to_device(torch.from_numpy(p).cuda(), dA, fused=True)
+    got = dA.cpu().numpy()
+    for b in range(2):
+        assert_close(got[b], O.apply_to(n, recs, p[b], A.copy()))
+    T = np.ascontiguousarray(A)
+    ev = sqg.CostEvaluator(c, T, trace_offset=N - cols)
+    cost, _ = ev.cost_grad(torch.from_numpy(p).cuda(), with_grad=False)
+    ref = [O.cost(n, recs, p[b], T, trace_offset=N - cols) for b in range(2)]
+    assert_close(cost.cpu().numpy(), np.array(ref))
