@@ -43,6 +43,7 @@ def lib():
         _lib.sqgr_apply_derivate_to.argtypes = [i, ip, i, dp, i, dp, i, i, i, dp]
         _lib.sqgr_combined_unitary.argtypes = [i, ip, i, dp, i, dp, i, dp, dp]
         _lib.sqgr_bfgs_run.argtypes = [i, ip, i, i, dp, i, i, i, dp, ctypes.c_long, dp, lp]
+        _lib.sqgr_tree_search.argtypes = [i, dp, i, i, i, ctypes.c_double, ctypes.c_longlong, ip, dp]
         _lib.sqgr_init()
     return _lib
 
@@ -155,3 +156,13 @@ def bfgs_run(qbit_num, gates, target, x0, max_iters, trace_offset=0, variant=0):
     _check(lib().sqgr_bfgs_run(qbit_num, gp, L, x.size, _dp(t.view(np.float64)), t.shape[1], trace_offset, variant,
                                _dp(x), max_iters, _dp(out), ctypes.byref(calls)), "bfgs_run")
     return x, float(out[0]), int(calls.value)
+
+
+def tree_search(qbit_num, target, use_osr=0, use_graph_search=0, level_max=14, tolerance=1e-8, seed=1):
+    """N_Qubit_Decomposition_Tree_Search on U^dagger: (CNOT count found, decomposition error)."""
+    t = _target(target)
+    cn = ctypes.c_int(0)
+    err = np.zeros(1)
+    _check(lib().sqgr_tree_search(qbit_num, _dp(t.view(np.float64)), use_osr, use_graph_search, level_max, tolerance,
+                                  seed, ctypes.byref(cn), _dp(err)), "tree_search")
+    return int(cn.value), float(err[0])

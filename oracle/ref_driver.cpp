@@ -16,6 +16,9 @@
  *   sqgr_apply_derivate_to Gates_block::apply_derivate_to (Gates_block.cpp:1012-1150)
  *   sqgr_combined_unitary Optimization_Interface::optimization_problem_combined_unitary
  *                        (wrapper :1446, Optimization_Interface.cpp:1525-1561)
+ *   sqgr_tree_search     N_Qubit_Decomposition_Tree_Search::start_decomposition
+ *                        (N_Qubit_Decomposition_Tree_Search.cpp, wrapper
+ *                        qgd_N_Qubit_Decompositions_Wrapper.cpp:401-460): CNOT count and error found
  *   sqgr_bfgs_run        one BFGS_Powell::Start_Optimization run on
  *                        Optimization_Interface::optimization_problem_combined, as one
  *                        iteration of solve_layer_optimization_problem_BFGS makes it
@@ -33,6 +36,7 @@
 
 #include "Gates_block.h"
 #include "N_Qubit_Decomposition_custom.h"
+#include "N_Qubit_Decomposition_Tree_Search.h"
 #include "BFGS_Powell.h"
 #include "config_element.h"
 
@@ -243,6 +247,39 @@ int sqgr_bfgs_run(int n, const int* g, int L, int P, double* udag, int cols, int
     } catch (...) {
         return 2;
     }
+}
+
+/* The reference's structure search on U^dagger (rows x rows) with all qubit pairs as the
+ * topology; use_osr / use_graph_search select its modes (0/0 is the exhaustive level search).
+ * Returns the CNOT count of the structure found and its decomposition error. */
+int sqgr_tree_search(int n, double* udag, int use_osr, int use_graph_search, int level_max, double tolerance,
+                     long long seed, int* cnots, double* error) {
+  try {
+    Matrix U(reinterpret_cast<QGD_Complex16*>(udag), 1 << n, 1 << n);
+    std::map<std::string, Config_Element> config;
+    auto put = [&](const char* key, long long v) {
+      Config_Element e;
+      e.set_property(key, v);
+      config[key] = e;
+    };
+    put("use_osr", use_osr);
+    put("use_graph_search", use_graph_search);
+    put("tree_level_max", level_max);
+    put("random_seed", seed);
+    Config_Element tol;
+    tol.set_property("optimization_tolerance", tolerance);
+    config["optimization_tolerance"] = tol;
+    N_Qubit_Decomposition_Tree_Search dec(U, n, config, 0);
+    dec.set_verbose(0);
+    dec.set_optimization_tolerance(tolerance);
+    dec.start_decomposition();
+    std::map<std::string, int> nums = dec.get_gate_nums();
+    *cnots = nums.count("CNOT") ? nums["CNOT"] : 0;
+    *error = dec.get_decomposition_error();
+    return 0;
+  } catch (...) {
+    return 2;
+  }
 }
 
 }  // extern "C"

@@ -201,7 +201,31 @@ def adaptive8():
           cost=np.array([a for a, _ in cg]), grad=np.stack([b for _, b in cg]), source="reference")
 
 
-JOBS = {"umtx4": umtx4, "adaptive8": adaptive8, "config1": config1, "config2": config2, "config3": config3, "config4": config4,
+def tree_search():
+    """The reference's structure search (N_Qubit_Decomposition_Tree_Search, all qubit pairs,
+    tolerance 1e-8, levels up to 8) in its default mode (operator-Schmidt-rank bounds with the
+    best-first graph search) and in its exhaustive level-search mode, on targets made from
+    random CNOT+U3 structures with k CNOTs.  Targets are stored as U^dagger padded to 16 x 16."""
+    rng = np.random.default_rng(8)
+    cases = [(2, 1), (2, 2), (2, 3), (3, 1), (3, 2), (3, 3), (3, 4), (4, 1), (4, 2)]
+    T = np.zeros((len(cases), 16, 16), dtype=np.complex128)
+    rows = []
+    for idx, (n, k) in enumerate(cases):
+        c = wl.cnot_u3_ansatz(n, k, pairs="random", rng=rng)
+        U = R.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
+        N = 1 << n
+        T[idx, :N, :N] = U.conj().T
+        d_cn, d_err = R.tree_search(n, T[idx, :N, :N], 1, 1, 8, 1e-8, 1)
+        e_cn, e_err = R.tree_search(n, T[idx, :N, :N], 0, 0, 8, 1e-8, 1)
+        rows.append((n, k, d_cn, d_err, e_cn, e_err))
+        print("tree search n=%d k=%d: default %d (%.1e), level search %d (%.1e)" % rows[-1], flush=True)
+    r = np.array(rows)
+    _save("tree_search_ref.npz", targets=T, qbit_num=r[:, 0].astype(int), generating_cnots=r[:, 1].astype(int),
+          default_cnots=r[:, 2].astype(int), default_error=r[:, 3], level_cnots=r[:, 4].astype(int),
+          level_error=r[:, 5], source="reference")
+
+
+JOBS = {"umtx4": umtx4, "adaptive8": adaptive8, "tree_search": tree_search, "config1": config1, "config2": config2, "config3": config3, "config4": config4,
         "config5": config5}
 
 if __name__ == "__main__":

@@ -308,3 +308,30 @@ def test_adam_budget_above_five_qubits_follows_the_reference(ts):
     assert cls._adam_budget(852) == 10000000
     assert cls._adam_budget(36) == int(36 / 852 * 10000000.0) == 422535
     assert cls._adam_budget(0) == 1
+
+
+def test_tree_search_finds_what_the_reference_finds(sqg):
+    """Targets made from random 1..4-CNOT structures at 2..4 qubits: the structure search finds a
+    decomposition with as many CNOTs as the reference's own search in its default mode found
+    (tests/golden/tree_search_ref.npz, made by running SQUANDER's N_Qubit_Decomposition_Tree_Search
+    built from its sources), within the tolerance.  The reference's exhaustive level search, the
+    mode this package restates, missed one of those minima (a 4-CNOT target solved with 5: its
+    one random start per candidate structure failed at level 4); the counts here may therefore be
+    lower than the reference's level-search counts, never higher than its default mode's."""
+    import os
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "tree_search_ref.npz"))
+    found = []
+    for idx in range(d["targets"].shape[0]):
+        n = int(d["qbit_num"][idx])
+        N = 1 << n
+        T = np.ascontiguousarray(d["targets"][idx, :N, :N])
+        dec = sqg.N_Qubit_Decomposition_Tree_Search(T, config={"optimization_tolerance": 1e-8, "random_seed": 1,
+                                                               "tree_level_max": 8})
+        dec.Start_Decomposition()
+        assert dec.get_Decomposition_Error() < 1e-8
+        found.append(len(dec.best_cnot_sequence))
+    found = np.array(found)
+    assert np.all(found <= d["default_cnots"]), (found, d["default_cnots"])
+    assert np.all(found <= d["level_cnots"]), (found, d["level_cnots"])
+    assert np.array_equal(found, d["default_cnots"]), (found, d["default_cnots"])
