@@ -310,6 +310,7 @@ def test_adam_budget_above_five_qubits_follows_the_reference(ts):
     assert cls._adam_budget(0) == 1
 
 
+@pytest.mark.gpu
 def test_tree_search_finds_what_the_reference_finds(sqg):
     """Targets made from random 1..4-CNOT structures at 2..4 qubits: the structure search finds a
     decomposition with as many CNOTs as the reference's own search in its default mode found
