@@ -27,6 +27,8 @@ def _install():
     part = importlib.import_module(_PKG + ".partitioning")
     qasm = importlib.import_module(_PKG + ".qasm")
     top = _module("squander", __path__=[], **{k: getattr(pkg, k) for k in pkg.__all__})
+    top.gates = _module("squander.gates", __path__=[])
+    top.gates.qgd_Circuit = _module("squander.gates.qgd_Circuit", qgd_Circuit=pkg.Circuit)
     top.utils = _module("squander.utils", qasm_to_squander_circuit=qasm.qasm_to_squander_circuit,
                         CompareCircuits=qasm.CompareCircuits)
     partitioning = _module("squander.partitioning", __path__=[])
