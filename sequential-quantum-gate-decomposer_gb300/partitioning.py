@@ -8,6 +8,7 @@ Public functions and the reference functions whose results they reproduce:
   total_float_ops             squander/partitioning/tools.py:84-108
   translate_param_order       squander/partitioning/tools.py:111-132
   PartitionCircuit            squander/partitioning/partition.py:50-91
+  (the optimal strategies: partitioning_ilp.max_partitions, squander/partitioning/ilp.py)
 
 How the greedy partitioner decides, stated as the rules this module implements:
 
@@ -35,9 +36,10 @@ How the greedy partitioner decides, stated as the rules this module implements:
 The result is identical to the reference's on the same circuit; the fixture
 tests/golden/partition_kahn.json, produced by running the reference's own modules, checks it.
 
-The ILP strategies ("ilp", "ilp-fusion", "ilp-fusion-ca") need the PuLP modelling package with
-the CBC or Gurobi solvers, and the "qiskit*" / "bqskit*" strategies need those frameworks; none
-of them is in this image, so PartitionCircuit raises NotImplementedError for them.
+The optimal strategies ("ilp", "ilp-fusion", "ilp-fusion-ca") are in partitioning_ilp.py and
+solve their models with SciPy's HiGHS in place of the reference's PuLP with CBC or Gurobi.  The
+"qiskit*" / "bqskit*" strategies need those frameworks, which this package does not include,
+so PartitionCircuit raises NotImplementedError for them.
 
 A partitioned circuit (a Circuit of sub-circuits) hands its block boundaries to the engine:
 the state-vector plan then starts fused passes only at partition boundaries, merging
@@ -238,10 +240,9 @@ def total_float_ops(num_qubit, max_qubits_per_partition, gate_to_qubit, gate_to_
     return (1 << spare if spare >= 0 else 0.5 ** -spare) * sum(per_block)
 
 
+_OPTIMAL = {"ilp": (False, False), "ilp-fusion": (True, False), "ilp-fusion-ca": (True, True)}
+
 _UNAVAILABLE = {
-    "ilp": "the PuLP modelling package with the CBC or Gurobi MILP solvers",
-    "ilp-fusion": "the PuLP modelling package with the CBC or Gurobi MILP solvers",
-    "ilp-fusion-ca": "the PuLP modelling package with the CBC or Gurobi MILP solvers",
     "qiskit": "Qiskit", "qiskit-fusion": "Qiskit",
     "bqskit-Quick": "BQSKit", "bqskit-Scan": "BQSKit", "bqskit-Greedy": "BQSKit", "bqskit-Cluster": "BQSKit",
 }
@@ -256,5 +257,11 @@ def PartitionCircuit(circ, parameters, max_partition_size, strategy="kahn", file
                                   "'kahn'" % (strategy, _UNAVAILABLE[strategy]))
     if strategy in ("tdag", "gtqcp"):
         raise NotImplementedError("partitioning strategy %r is not restated; use 'kahn'" % strategy)
-    partitioned, param_order, parts = kahn_partition(circ, max_partition_size)
+    if strategy in _OPTIMAL:
+        from .partitioning_ilp import max_partitions
+
+        fusion_cost, control_aware = _OPTIMAL[strategy]
+        partitioned, param_order, parts = max_partitions(circ, max_partition_size, fusion_cost, control_aware)
+    else:
+        partitioned, param_order, parts = kahn_partition(circ, max_partition_size)
     return partitioned, translate_param_order(parameters, param_order), parts

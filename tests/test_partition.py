@@ -97,8 +97,9 @@ def test_partitioned_circuit_computes_the_same_operator(sqg, part, n, count, mq)
 def test_partition_strategies_and_flop_model(sqg, part):
     c = sqg.Circuit(3)
     c.add_CNOT(0, 1)
-    with pytest.raises(NotImplementedError, match="PuLP"):
-        part.PartitionCircuit(c, np.zeros(0), 2, strategy="ilp-fusion")
+    for strategy in ("ilp", "ilp-fusion", "ilp-fusion-ca"):
+        pc, _, parts = part.PartitionCircuit(c, np.zeros(0), 2, strategy=strategy)
+        assert parts == [[0]]
     with pytest.raises(NotImplementedError, match="Qiskit"):
         part.PartitionCircuit(c, np.zeros(0), 2, strategy="qiskit")
     # unknown names fall back to kahn, as in the reference
