@@ -18,7 +18,9 @@ except the BLAS routines, which stay OpenBLAS:
   ``LAPACKE_zgesdd``/``cgesdd`` forwarded to the OpenBLAS build bundled with numpy.
 
 Kernels are the reference's portable ones (no ``USE_AVX``), so the same recipe works on
-x86-64 and arm64.  The reference tree is found at ``$SQG_REFERENCE_ROOT`` or
+x86-64 and arm64.  ``build(avx=True)`` (x86-64 only) builds a second library,
+``oracle/_ref/libsqg_ref_avx.so``, with the reference's AVX kernels and ``-O3 -mavx2 -mfma``,
+as its own CMake build does on x86; it serves timing comparisons, not parity.  The reference tree is found at ``$SQG_REFERENCE_ROOT`` or
 ``/root/reference``; without it ``build()`` returns None and the tests that need the
 library skip.
 
@@ -27,6 +29,7 @@ Usage: ``python oracle/build_ref.py`` (or ``build()`` from the tests).
 import concurrent.futures as cf
 import glob
 import os
+import platform
 import subprocess
 import sys
 
@@ -52,13 +55,13 @@ def reference_root():
     return src if os.path.isdir(src) else None
 
 
-def _sources(src):
+def _sources(src, avx=False):
     files = []
     for f in sorted(glob.glob(os.path.join(src, "common", "*.cpp"))):
         if not any(x in os.path.basename(f) for x in _EXCLUDE):
             files.append(f)
     files += sorted(glob.glob(os.path.join(src, "gates", "*.cpp")))
-    files += [f for f in sorted(glob.glob(os.path.join(src, "gates", "kernels", "*.cpp"))) if "AVX" not in f]
+    files += [f for f in sorted(glob.glob(os.path.join(src, "gates", "kernels", "*.cpp"))) if avx or "AVX" not in f]
     for d in ("decomposition", "optimization_engines", "random_unitary", "nn"):
         files += sorted(glob.glob(os.path.join(src, d, "*.cpp")))
     return files
@@ -73,10 +76,11 @@ def _openblas():
     return os.path.realpath(libs[0])
 
 
-def _flags(src):
+def _flags(src, avx=False):
     inc = ["-I" + SHIM] + ["-I" + os.path.join(src, d, "include") for d in _SUBDIRS_INC]
     # -include climits: Optimization_Interface.cpp uses INT_MAX without including <climits>
-    return ["-std=c++17", "-O2", "-fPIC", "-fopenmp", "-w", "-include", "climits"] + inc
+    opt = ["-O3", "-DUSE_AVX", "-mavx2", "-mfma"] if avx else ["-O2"]
+    return ["-std=c++17", "-fPIC", "-fopenmp", "-w", "-include", "climits"] + opt + inc
 
 
 def _compile(args):
@@ -87,21 +91,24 @@ def _compile(args):
     return None if r.returncode == 0 else (f, r.stderr[-2000:])
 
 
-def build(force=False, verbose=False):
-    """Build oracle/_ref/libsqg_ref.so; returns its path, or None without the reference tree."""
+def build(force=False, verbose=False, avx=False):
+    """Build oracle/_ref/libsqg_ref.so (libsqg_ref_avx.so with avx=True); returns its path, or
+    None without the reference tree (or, for avx, on a host that is not x86-64)."""
     src = reference_root()
-    if src is None:
+    if src is None or (avx and platform.machine() not in ("x86_64", "AMD64")):
         return None
+    lib_path = LIB_PATH.replace(".so", "_avx.so") if avx else LIB_PATH
+    obj_dir = OBJ_DIR + "_avx" if avx else OBJ_DIR
     deps = [DRIVER, os.path.join(SHIM, "blas_shim.cpp"), __file__] + glob.glob(os.path.join(SHIM, "tbb", "*.h"))
-    if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(d) for d in deps)):
-        return LIB_PATH
-    os.makedirs(OBJ_DIR, exist_ok=True)
-    flags = _flags(src)
+    if (not force and os.path.exists(lib_path)
+            and os.path.getmtime(lib_path) >= max(os.path.getmtime(d) for d in deps)):
+        return lib_path
+    os.makedirs(obj_dir, exist_ok=True)
+    flags = _flags(src, avx)
     jobs = []
-    for f in _sources(src) + [DRIVER, os.path.join(SHIM, "blas_shim.cpp")]:
+    for f in _sources(src, avx) + [DRIVER, os.path.join(SHIM, "blas_shim.cpp")]:
         tag = os.path.relpath(f, src).replace(os.sep, "_") if f.startswith(src) else "local_" + os.path.basename(f)
-        jobs.append((f, os.path.join(OBJ_DIR, tag[:-4] + ".o"), flags))
+        jobs.append((f, os.path.join(obj_dir, tag[:-4] + ".o"), flags))
     if force:
         for _, obj, _ in jobs:
             if os.path.exists(obj):
@@ -111,16 +118,16 @@ def build(force=False, verbose=False):
     if errors:
         raise RuntimeError("reference build failed:\n" + "\n".join("%s\n%s" % e for e in errors))
     blas = _openblas()
-    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    tmp = lib_path + ".tmp%d" % os.getpid()
     subprocess.check_call(["g++", "-shared", "-fopenmp", "-o", tmp] + [o for _, o, _ in jobs]
                           + [blas, "-Wl,-rpath," + os.path.dirname(blas), "-Wl,--no-undefined"])
-    os.replace(tmp, LIB_PATH)
+    os.replace(tmp, lib_path)
     if verbose:
-        print("built", LIB_PATH, "from", len(jobs), "translation units")
-    return LIB_PATH
+        print("built", lib_path, "from", len(jobs), "translation units")
+    return lib_path
 
 
 if __name__ == "__main__":
-    path = build(force="--force" in sys.argv, verbose=True)
+    path = build(force="--force" in sys.argv, verbose=True, avx="--avx" in sys.argv)
     if path is None:
         sys.exit("reference tree not found (set SQG_REFERENCE_ROOT)")

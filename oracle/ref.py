@@ -7,9 +7,11 @@ for the GPU tests.  It exists only where the reference tree exists; ``available(
 whether it could be built.
 
 The call signatures follow ``oracle.py`` (gate records ``(type, target, control,
-param_start)``, complex128 matrices, U^dagger as the target).
+param_start)``, complex128 matrices, U^dagger as the target).  With ``SQG_REF_AVX=1`` it loads
+the reference's AVX build instead (x86-64 only; for timing comparisons).
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -27,7 +29,7 @@ def lib():
     global _lib, _tried
     if _lib is None and not _tried:
         _tried = True
-        path = build_ref.build()
+        path = build_ref.build(avx=os.environ.get("SQG_REF_AVX") == "1")
         if path is None:
             return None
         _lib = ctypes.CDLL(path)
