@@ -18,8 +18,9 @@ Its Adaptive gate is a CRY whose angle passes through activation_function
 engine's CRY.  Every inner decomposition is an N_Qubit_Decomposition_custom run on the device
 (BFGS up to five qubits, ADAM above, with the reference's budgets).  The candidates of one
 compression step (the circuit without one of its blocks, all with the same gate types) are
-decomposed together in one launch (sqg_decompose_structures); the reference runs them one after
-another.  Random choices (randomized layer order, the subset of blocks tried, ties of the
+decomposed together in one launch, one CTA each: sqg_decompose_structures (BFGS) up to five
+qubits, sqg_decompose_structures_adam at six qubits when there are at least batch_adam_min of
+them; the reference runs them one after another.  Random choices (randomized layer order, the subset of blocks tried, ties of the
 penalty) come from the decomposer's seeded generator instead of the reference's std::mt19937.
 """
 import math
@@ -151,6 +152,72 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
         self.Umtx = np.ascontiguousarray(self.Umtx * factor)
         self._evaluator = None
 
+    # candidates of one step from which six-qubit ADAM decompositions run one CTA each in a
+    # single launch (sqg_decompose_structures_adam) instead of one whole-GPU graph launch each
+    batch_adam_min = 4
+
+    def _stage_budget(self, stage, adam, P):
+        """Evaluation budget of a stage's custom decompositions.  The reference copies
+        max_inner_iterations_compression / _final into the stage's config as
+        max_inner_iterations (N_Qubit_Decomposition_adaptive.cpp:574-579, 1269-1275); the
+        engines read max_inner_iterations_bfgs / _adam, then max_inner_iterations
+        (BFGS.cpp:91-97, ADAM.cpp:98-103), before the value the stage sets: BFGS 10000 (100
+        for compression), ADAM P / 852 * 1e7 (100000 for compression), :600-616, :1303-1313."""
+        cfg = self.config
+        own = "max_inner_iterations_adam" if adam else "max_inner_iterations_bfgs"
+        key = {"compression": "max_inner_iterations_compression", "final": "max_inner_iterations_final"}.get(stage)
+        if own in cfg:
+            return int(cfg[own])
+        if key and key in cfg:
+            return int(cfg[key])
+        if "max_inner_iterations" in cfg:
+            return int(cfg["max_inner_iterations"])
+        if adam:
+            return 100000 if stage == "compression" else int(P / 852 * 10000000.0)
+        return 100 if stage == "compression" else 10000
+
+    def _adam_settings(self, stage, tol):
+        """ADAM engine settings of a stage: (tolerance, eta, adaptive eta, random shifts at most,
+        randomization threshold), with the config keys ADAM.cpp:98-170 reads."""
+        cfg = self.config
+        tol_a = float(cfg.get("optimization_tolerance_adam", tol))
+        eta = float(cfg["eta"]) if "eta" in cfg else 1e-3
+        adaptive = bool(cfg["adaptive_eta"]) if "adaptive_eta" in cfg else True
+        thr = int(cfg.get("randomization_threshold_adam", cfg.get("randomization_threshold", 2500000)))
+        shifts = 1 if stage == "compression" else 10000
+        return tol_a, eta, adaptive, shifts, thr
+
+    def _groups(self, structs):
+        groups = {}
+        for i, s in enumerate(structs):
+            groups.setdefault(s.types(), []).append(i)
+        return groups
+
+    def _start_points(self, structs, starts, idx, P):
+        return np.stack([starts[i] if starts[i] is not None else self.rng.uniform(0, 2 * math.pi, P) for i in idx])
+
+    def _inner_adam_batched(self, structs, starts, idx, stage, tol, max_outer, out):
+        """The ADAM decompositions of structures idx (same gate types, six qubits) in one
+        launch, one CTA each (sqg_decompose_structures_adam)."""
+        nc = structs[idx[0]].circuit().native()
+        P, B = nc.param_num, len(idx)
+        target = self.evaluator().target
+        tol_a, eta, adaptive, shifts, thr = self._adam_settings(stage, tol)
+        recs = np.ascontiguousarray(np.stack([structs[i].records() for i in idx]))
+        x = dev.to_device_real(self._start_points(structs, starts, idx, P))
+        cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
+        evals = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
+        lib = _native.lib()
+        w = dev.Workspace().get(lib.sqg_decompose_structures_adam_workspace_bytes(nc.handle, B))
+        _native.check(lib.sqg_decompose_structures_adam(
+            nc.handle, recs.ctypes.data, dev.ptr(target), 0, target.shape[1], B, self.trace_offset, self.cost_variant,
+            dev.ptr(x), dev.ptr(cost), dev.ptr(evals), None, tol_a, self._stage_budget(stage, True, P), eta,
+            1 if adaptive else 0, shifts, thr, max_outer, int(self.rng.integers(1 << 62)), dev.ptr(w), w.numel(),
+            dev.stream_ptr()), "sqg_decompose_structures_adam")
+        c, xs, ev = cost.cpu().numpy(), x.cpu().numpy(), evals.cpu().numpy()
+        for j, i in enumerate(idx):
+            out[i] = (float(c[j]), xs[j].copy(), int(ev[j]))
+
     def _inner(self, structs, starts, stage, tol):
         """One custom decomposition per (structure, start point or None for a random start).
         Returns [(minimum, best point, evaluations)]."""
@@ -159,22 +226,15 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
         loops = int(self.config.get("max_iteration_loops", 3 if n == 2 else 1))
         out = [None] * len(structs)
         if n <= 5:
-            max_inner = {"initial": 10000, "compression": 100, "final": 10000}[stage]
-            key = {"compression": "max_inner_iterations_compression", "final": "max_inner_iterations_final"}.get(stage)
-            if key and key in self.config:
-                max_inner = int(self.config[key])
-            groups = {}
-            for i, s in enumerate(structs):
-                groups.setdefault(s.types(), []).append(i)
+            groups = self._groups(structs)
             target = self.evaluator().target
             lib = _native.lib()
             for idx in groups.values():
                 nc = structs[idx[0]].circuit().native()
                 P, B = nc.param_num, len(idx)
+                max_inner = self._stage_budget(stage, False, P)
                 recs = np.ascontiguousarray(np.stack([structs[i].records() for i in idx]))
-                x0 = np.stack([starts[i] if starts[i] is not None else self.rng.uniform(0, 2 * math.pi, P)
-                               for i in idx])
-                x = dev.to_device_real(x0)
+                x = dev.to_device_real(self._start_points(structs, starts, idx, P))
                 cost = dev.torch.empty(B, dtype=dev.torch.float64, device="cuda")
                 calls = dev.torch.empty(B, dtype=dev.torch.int32, device="cuda")
                 w = dev.Workspace().get(lib.sqg_decompose_structures_workspace_bytes(nc.handle, B, target.shape[1]))
@@ -187,11 +247,18 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
                 for j, i in enumerate(idx):
                     out[i] = (float(c[j]), xs[j].copy(), int(ev[j]))
             return out
-        for i, s in enumerate(structs):  # ADAM above five qubits, one graph launch per run
+        single = list(range(len(structs)))
+        if n == 6:
+            for idx in self._groups(structs).values():
+                if len(idx) >= self.batch_adam_min:
+                    self._inner_adam_batched(structs, starts, idx, stage, tol, max_outer, out)
+            single = [i for i in single if out[i] is None]
+        for i in single:  # ADAM above five qubits, one graph launch per run
+            s = structs[i]
             P = s.param_num()
             cfg = dict(self.config)
-            cfg["max_inner_iterations"] = {"initial": int(P / 852 * 10000000.0), "compression": 100000,
-                                           "final": int(P / 852 * 10000000.0)}[stage]
+            cfg.pop("max_inner_iterations_adam", None)
+            cfg["max_inner_iterations"] = self._stage_budget(stage, True, P)
             cfg["random_shift_count_max"] = 1 if stage == "compression" else 10000
             cfg["optimization_tolerance"] = tol
             d = N_Qubit_Decomposition_custom(self.Umtx, self.qbit_num, None, cfg)

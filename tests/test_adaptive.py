@@ -121,3 +121,53 @@ def test_state_preparation_maps_the_state_to_zero(sqg):
     assert sp.get_Decomposition_Error() < 1e-8
     C = O.get_matrix(3, sp.get_Circuit().gate_records(), sp.get_Optimized_Parameters())
     assert abs(abs((C @ psi)[0]) - 1.0) < 1e-8
+
+
+def test_stage_budgets_follow_the_reference_precedence(ad):
+    """max_inner_iterations_bfgs / _adam, then the stage's own key, then max_inner_iterations,
+    then the stage's value (N_Qubit_Decomposition_adaptive.cpp:574-616, 1269-1313)."""
+    d = _dec(ad)
+    assert [d._stage_budget(s, False, 93) for s in ("initial", "compression", "final")] == [10000, 100, 10000]
+    assert [d._stage_budget(s, True, 852) for s in ("initial", "compression", "final")] == [10000000, 100000,
+                                                                                              10000000]
+    d.config = {"max_inner_iterations": 7, "max_inner_iterations_compression": 5}
+    assert [d._stage_budget(s, False, 93) for s in ("initial", "compression", "final")] == [7, 5, 7]
+    d.config["max_inner_iterations_adam"] = 3
+    assert [d._stage_budget(s, True, 93) for s in ("initial", "compression", "final")] == [3, 3, 3]
+    assert [d._stage_budget(s, False, 93) for s in ("initial", "compression", "final")] == [7, 5, 7]
+
+
+@pytest.mark.gpu
+def test_six_qubit_compression_candidates_run_in_one_adam_launch(sqg, ad):
+    """At six qubits the candidates of a compression step (the circuit without one of its
+    blocks) run as one sqg_decompose_structures_adam launch: each candidate's result equals, bit
+    for bit, a batched ADAM run of its own structure from the same start with the same seed (the
+    stage's settings: the compression budget from the config, one random shift), and the
+    evaluations stop at that budget."""
+    torch = pytest.importorskip("torch")
+    import copy
+
+    n, budget = 6, 60
+    builder = ad.N_Qubit_Decomposition_adaptive(np.eye(64, dtype=np.complex128), config={"random_seed": 2})
+    s = ad._Structure(n, builder._adaptive_layer()[:6] + [builder._final_layer()])
+    rng = np.random.default_rng(61)
+    theta = rng.uniform(0, 2 * np.pi, s.param_num())
+    T = np.ascontiguousarray(O.get_matrix(n, s.records(), theta).conj().T)
+    dec = ad.N_Qubit_Decomposition_adaptive(T, config={"optimization_tolerance": 1e-8, "random_seed": 9,
+                                                       "max_inner_iterations_compression": budget})
+    cands = [s.without(b) for b in range(5)]
+    starts = [dec._reduced(s, theta, b) for b in range(5)]
+    state = copy.deepcopy(dec.rng.bit_generator.state)
+    out = dec._inner(cands, starts, "compression", 1e-8)
+    replay = np.random.default_rng()
+    replay.bit_generator.state = state
+    seed = int(replay.integers(1 << 62))
+    targets = torch.from_numpy(np.stack([T] * len(cands))).cuda()
+    for k, cand in enumerate(cands):
+        bd = sqg.BatchedDecomposer(cand.circuit(), tolerance=1e-8, max_calls=budget, max_outer=1, optimizer="ADAM",
+                                   eta=1e-3, random_shift_count_max=1)
+        xk, ck, ek = bd.run(targets, np.stack(starts), seed=seed)
+        torch.cuda.synchronize()
+        f, x, ev = out[k]
+        assert float(ck[k]) == f and np.array_equal(xk[k].cpu().numpy(), x) and int(ek[k]) == ev
+        assert ev <= budget
