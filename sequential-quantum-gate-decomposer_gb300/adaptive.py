@@ -472,13 +472,64 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
             blocks.append(nb)
         return _Structure(self.qbit_num, blocks), np.asarray(xs, dtype=np.float64)
 
-    def Start_Decomposition(self):
-        """start_decomposition: the initial circuit, its compression, its finalisation."""
+    # ---- the stages as the reference's wrapper exposes them --------------------------------
+    def _held(self):
+        """The gate structure the decomposer holds (built by add_Adaptive_Layers /
+        add_Finalyzing_Layer_To_Gate_Structure, or left by an earlier stage), one block per
+        top-level item, with its parameters (None when they do not fit it)."""
+        c = self.circuit
+        s = _Structure(self.qbit_num, [list(c._gates[a:b]) for a, b in c._item_ranges()])
+        x = self.optimized_parameters
+        return s, (x.copy() if x is not None and x.size == s.param_num() else None)
+
+    def _hold(self, s, x):
+        self.structure = s
+        self.circuit = s.circuit()
+        self._evaluator = None
+        self.optimized_parameters = np.asarray(x, dtype=np.float64)
+        self.decomposition_error = self.Optimization_Problem(self.optimized_parameters)
+
+    def _final_tolerance(self):
+        """finalize_circuit reads the config's optimization_tolerance into an integer
+        (N_Qubit_Decomposition_adaptive.cpp:538-543; Config_Element keeps a float entry's integer
+        field at 0), so a float entry makes the final tolerance 0 and the final optimisation runs
+        its whole budget; an integer entry is used as it is; without one the tolerance is 1e-4."""
+        v = self.config.get("optimization_tolerance")
+        if v is None:
+            return 1e-4
+        if isinstance(v, (int, np.integer)) and not isinstance(v, bool):
+            return float(v)
+        return 0.0
+
+    def get_Initial_Circuit(self):
+        """get_initial_circuit (:289-370): nothing when level_limit is 0; with a gate structure
+        already held, one decomposition of it from the held parameters
+        (optimize_imported_gate_structure, :687-776); otherwise the level search of
+        determine_initial_gate_structure.  The result is held for the next stage."""
         if self.level_limit == 0:
-            print("please increase level limit")
             return 0
         tol = float(self.config.get("optimization_tolerance", self.optimization_tolerance))
-        f, s, x = self._initial(tol)
+        if self.circuit.get_Gate_Num() > 0:
+            s, x0 = self._held()
+            f, x, ev = self._inner([s], [x0], "initial", tol)[0]
+            self.num_iters += ev
+        else:
+            f, s, x = self._initial(tol)
+        self._current_minimum = f
+        self._hold(s, x)
+        return 0
+
+    def Compress_Circuit(self):
+        """compress_circuit (:372-497): rounds of compress_gate_structure while fewer than 25
+        rounds ran or at most five rounds in a row removed nothing, stopping after the second
+        such round; nothing without a held gate structure."""
+        if self.circuit.get_Gate_Num() == 0:
+            return 0
+        tol = float(self.config.get("optimization_tolerance", self.optimization_tolerance))
+        s, x = self._held()
+        if x is None:
+            x = self.rng.uniform(0, 2 * math.pi, s.param_num())
+        f = getattr(self, "_current_minimum", math.inf)
         it, unc = 0, 0
         while it < 25 or unc <= 5:
             s2, x2, f2 = self._compress(s, x, f, unc, tol)
@@ -488,15 +539,35 @@ class N_Qubit_Decomposition_adaptive(N_Qubit_Decomposition_custom):
             if unc > 1:
                 break
         self.compressed_structure = s
+        self._current_minimum = f
+        self._hold(s, x)
+        return 0
+
+    def Finalize_Circuit(self):
+        """finalize_circuit (:499-685): the controlled rotations replaced by CNOT / CZ
+        constructions (replace_trivial_CRY_gates) and one final decomposition from the held
+        parameters; nothing without a held gate structure."""
+        if self.circuit.get_Gate_Num() == 0:
+            return 0
+        s, x = self._held()
+        if x is None:
+            x = np.zeros(s.param_num())
         s, x = self._replace_trivial_cry(s, x)
-        tol_final = float(self.config.get("optimization_tolerance", 1e-4))
-        f, x, ev = self._inner([s], [x], "final", tol_final)[0]
+        f, x, ev = self._inner([s], [x], "final", self._final_tolerance())[0]
         self.num_iters += ev
-        self.structure = s
-        self.circuit = s.circuit()
-        self._evaluator = None
-        self.optimized_parameters = x
-        self.decomposition_error = self.Optimization_Problem(x)
+        self._current_minimum = f
+        self._hold(s, x)
+        return 0
+
+    def Start_Decomposition(self):
+        """start_decomposition (:245-260): get_Initial_Circuit, Compress_Circuit,
+        Finalize_Circuit."""
+        if self.level_limit == 0:
+            print("please increase level limit")
+            return 0
+        self.get_Initial_Circuit()
+        self.Compress_Circuit()
+        self.Finalize_Circuit()
         return 0
 
 

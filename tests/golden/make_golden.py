@@ -205,14 +205,21 @@ def tree_search():
     """The reference's structure search (N_Qubit_Decomposition_Tree_Search, all qubit pairs,
     tolerance 1e-8, levels up to 8) in its default mode (operator-Schmidt-rank bounds with the
     best-first graph search) and in its exhaustive level-search mode, on targets made from
-    random CNOT+U3 structures with k CNOTs.  Targets are stored as U^dagger padded to 16 x 16."""
+    random CNOT+U3 structures with k CNOTs, and on the reference's own 4-qubit test target
+    data/Umtx.mat (the last entry, k = -1).  Targets are stored as U^dagger padded to 16 x 16."""
+    import scipy.io
+
     rng = np.random.default_rng(8)
-    cases = [(2, 1), (2, 2), (2, 3), (3, 1), (3, 2), (3, 3), (3, 4), (4, 1), (4, 2)]
+    cases = [(2, 1), (2, 2), (2, 3), (3, 1), (3, 2), (3, 3), (3, 4), (4, 1), (4, 2), (4, -1)]
     T = np.zeros((len(cases), 16, 16), dtype=np.complex128)
     rows = []
     for idx, (n, k) in enumerate(cases):
-        c = wl.cnot_u3_ansatz(n, k, pairs="random", rng=rng)
-        U = R.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
+        if k < 0:
+            src = R.build_ref.reference_root()
+            U = scipy.io.loadmat(os.path.join(src, "..", "..", "data", "Umtx.mat"))["Umtx"].astype(np.complex128)
+        else:
+            c = wl.cnot_u3_ansatz(n, k, pairs="random", rng=rng)
+            U = R.get_matrix(n, c.gate_records(), rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()))
         N = 1 << n
         T[idx, :N, :N] = U.conj().T
         d_cn, d_err = R.tree_search(n, T[idx, :N, :N], 1, 1, 8, 1e-8, 1)

@@ -312,7 +312,8 @@ def test_adam_budget_above_five_qubits_follows_the_reference(ts):
 
 @pytest.mark.gpu
 def test_tree_search_finds_what_the_reference_finds(sqg):
-    """Targets made from random 1..4-CNOT structures at 2..4 qubits: the structure search finds a
+    """Targets made from random 1..4-CNOT structures at 2..4 qubits, and the reference's own
+    4-qubit test target data/Umtx.mat: the structure search finds a
     decomposition with as many CNOTs as the reference's own search in its default mode found
     (tests/golden/tree_search_ref.npz, made by running SQUANDER's N_Qubit_Decomposition_Tree_Search
     built from its sources), within the tolerance.  The reference's exhaustive level search, the
