@@ -57,7 +57,8 @@ class _Items:
         self.items = list(circuit.get_Gates())
         count = len(self.items)
         self.qubits = [frozenset(it.get_Involved_Qbits()) for it in self.items]
-        self.target = [it.get_Target_Qbit() for it in self.items]
+        # a sub-circuit item has no target qubit of its own
+        self.target = [it.get_Target_Qbit() if hasattr(it, "get_Target_Qbit") else -1 for it in self.items]
         self.succ = [set() for _ in range(count)]
         self.pred = [set() for _ in range(count)]
         for i, it in enumerate(self.items):
