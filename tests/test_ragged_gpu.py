@@ -51,6 +51,24 @@ def test_ragged_matches_oracle(mods, variant):
     assert np.allclose(cost_only.cpu().numpy(), cost, atol=1e-13)
 
 
+def test_ragged_large_instances_match_oracle(mods):
+    """Instances of 8, 9 and 10 qubits beside small ones in one launch (the uneven batches span
+    3 to 10 qubits): cost and gradient against the oracle at 1e-12."""
+    rg, wl = mods
+    rng = np.random.default_rng(97)
+    circs, targets = make_instances(wl, rng, [8, 3, 10, 9])
+    rb = rg.RaggedBatch(circs, targets)
+    thetas = [rng.uniform(0, 2 * np.pi, c.get_Parameter_Num()) for c in circs]
+    cost, grad = rb.cost_grad(rb.pack(thetas))
+    torch.cuda.synchronize()
+    cost = cost.cpu().numpy()
+    grads = [g.cpu().numpy() for g in rb.split(grad)]
+    for i, c in enumerate(circs):
+        rc, rgd = O.cost_grad(c.qbit_num, c.gate_records(), thetas[i], targets[i])
+        assert abs(cost[i] - rc) <= 1e-12 * max(1.0, abs(rc))
+        assert np.max(np.abs(grads[i] - rgd)) <= 1e-12 * max(1.0, np.max(np.abs(rgd)))
+
+
 def test_tile_override_and_graph_replay(mods):
     rg, wl = mods
     rng = np.random.default_rng(95)
