@@ -179,11 +179,12 @@ def bfgs_flops_per_iteration(P):
 
 # DRAM bytes of one k_decompose launch of the timed workload (4096 targets), measured once with
 # ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (one pass, --profile-case decompose_full)
-K_DECOMPOSE_DRAM_BYTES = 26.63e9 + 78.01e9
+K_DECOMPOSE_DRAM_BYTES = 25.60e9 + 45.09e9
 K_DECOMPOSE_TRAFFIC_SOURCE = ("dram__bytes_read.sum + dram__bytes_write.sum of one k_decompose launch of this "
-                              "workload (ncu, one pass): 26.63 GB read, 78.01 GB written; L2 writes back the BFGS "
-                              "matrices although their 1216 resident slots (84 MB) fit in it, and the out-of-line "
-                              "evaluation spills registers to local memory")
+                              "workload (ncu): 25.60 GB read, 45.09 GB written; the BFGS matrices are kept in L2 "
+                              "with the evict_last policy (78 GB written without it), and what reaches HBM is "
+                              "mostly the out-of-line evaluation's register spills, whose local-memory window "
+                              "(about 140 MB) does not fit in L2 beside them")
 
 
 def decomposition_steps(torch, decs, streams, flush, tdev, start_fn, seeds):

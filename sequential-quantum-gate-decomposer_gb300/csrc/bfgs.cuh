@@ -25,6 +25,28 @@ struct BfgsVecs {
   double *redd, *scratch;
 };
 
+// Accessors of the Z matrix.  ZMem: plain loads and stores (Z in shared memory, or global).
+// ZKeepL2: Z in global memory, every load and store carrying an L2 evict_last policy, so
+// that the matrices of the resident CTAs stay in L2 rather than being written back to HBM
+// between the passes of one iteration.  The address must point to global memory.
+struct ZMem {
+  __device__ __forceinline__ double ld(const double* p) const { return *p; }
+  __device__ __forceinline__ void st(double* p, double v) const { *p = v; }
+};
+
+struct ZKeepL2 {
+  unsigned long long pol;
+  __device__ __forceinline__ ZKeepL2() { asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol)); }
+  __device__ __forceinline__ double ld(const double* p) const {
+    double v;
+    asm volatile("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol) : "memory");
+    return v;
+  }
+  __device__ __forceinline__ void st(double* p, double v) const {
+    asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(pol) : "memory");
+  }
+};
+
 static __device__ __forceinline__ double u01(unsigned long long k) {
   unsigned long long z = k + 0x9E3779B97F4A7C15ULL;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
@@ -103,7 +125,8 @@ static __device__ __forceinline__ int block_allmax_int(int v, double* scratch) {
 //   y'_col = alpha_col * sum_{i>=col} y_i z_i - beta_col * y_{col-1},
 //   alpha_col = z_{col-1} / (r_{col-1} r_col),  beta_col = r_col / r_{col-1}.
 // Keeping alpha_col as the column's new scale leaves two FP64 operations per entry.
-static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
+template <class ZA>
+static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z, const ZA& za) {
   double* Z = sh.Z;
   double red[4] = {0.0, 0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -118,7 +141,7 @@ static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
   for (int c = threadIdx.x; c < P; c += blockDim.x) {
     double s = 0.0;
 #pragma unroll 8
-    for (int r = 0; r < P; r++) s = fma(Z[(long long)r * P + c], sh.g[r], s);
+    for (int r = 0; r < P; r++) s = fma(za.ld(Z + (long long)r * P + c), sh.g[r], s);
     sh.v[c] = s * sh.cs[c];
   }
   block_allsum_n(red, sh.redd);
@@ -172,11 +195,11 @@ static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
   for (int r = threadIdx.x; r < P; r += blockDim.x) {
     double* row = Z + (long long)r * P;
     if (m < 1) break;
-    double sd = 0.0, ycur = row[m];
+    double sd = 0.0, ycur = za.ld(row + m);
     for (int col = m; col >= 1; col -= kChunk) {
       double yp[kChunk], out[kChunk];
 #pragma unroll
-      for (int j = 0; j < kChunk; j++) yp[j] = col - 1 - j >= 0 ? row[col - 1 - j] : 0.0;
+      for (int j = 0; j < kChunk; j++) yp[j] = col - 1 - j >= 0 ? za.ld(row + col - 1 - j) : 0.0;
       if (!zero_alpha) {
 #pragma unroll
         for (int j = 0; j < kChunk; j++) {
@@ -196,7 +219,7 @@ static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
       }
 #pragma unroll
       for (int j = 0; j < kChunk; j++)
-        if (col - j >= 1) row[col - j] = out[j];
+        if (col - j >= 1) za.st(row + col - j, out[j]);
     }
   }
   if (norm_Z < 0.0) {
@@ -211,7 +234,7 @@ static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
   double c0 = 0.0;
   for (int r = threadIdx.x; r < P; r += blockDim.x) {
     const double z0 = fabs(sh.delta[r]) > kNumPrecision ? sh.delta[r] * isdt : 0.0;
-    Z[(long long)r * P] = z0;
+    za.st(Z + (long long)r * P, z0);
     c0 = fma(z0, sh.g[r], c0);
   }
   for (int col = threadIdx.x + 1; col <= m; col += blockDim.x) sh.cs[col] = zero_alpha ? 1.0 : sh.nz[col];
@@ -229,7 +252,7 @@ static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
     for (int r0 = 0; r0 < P; r0 += kChunk) {
       double zv[kChunk];
 #pragma unroll
-      for (int j = 0; j < kChunk; j++) zv[j] = r0 + j < P ? Z[(long long)(r0 + j) * P + c] : 0.0;
+      for (int j = 0; j < kChunk; j++) zv[j] = r0 + j < P ? za.ld(Z + (long long)(r0 + j) * P + c) : 0.0;
 #pragma unroll
       for (int j = 0; j < kChunk; j++) {
         if (r0 + j < P) {
@@ -239,7 +262,7 @@ static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
       }
 #pragma unroll
       for (int j = 0; j < kChunk; j++)
-        if (r0 + j < P) Z[(long long)(r0 + j) * P + c] = zv[j];
+        if (r0 + j < P) za.st(Z + (long long)(r0 + j) * P + c, zv[j]);
     }
     const double nzc = s * cs * cs;
     const double sc = (nzc < norm_Z && nzc > kNumPrecision) ? sqrt(norm_Z / nzc) : 1.0;
@@ -255,13 +278,15 @@ static __device__ double bfgs_update(int P, const BfgsVecs& sh, double norm_Z) {
 // Search direction d = -Z Z^T g with Z = Zs diag(cs) (get_search_direction,
 // BFGS_Powell.cpp:407-446); Z^T g (ztg) and cs * Z^T g (zs) come from the last update or, for
 // Z = I, are g itself.  Returns d.g, the maximal step and g.g.
-static __device__ void bfgs_direction(int P, const BfgsVecs& sh, double& dg, double& max_step, double& gn) {
+template <class ZA>
+static __device__ void bfgs_direction(int P, const BfgsVecs& sh, double& dg, double& max_step, double& gn,
+                                      const ZA& za) {
   const double* Z = sh.Z;
   for (int r = threadIdx.x; r < P; r += blockDim.x) {
     const double* row = Z + (long long)r * P;
     double s = 0.0;
 #pragma unroll 8
-    for (int c = 0; c < P; c++) s = fma(-row[c], sh.zs[c], s);
+    for (int c = 0; c < P; c++) s = fma(-za.ld(row + c), sh.zs[c], s);
     sh.d[r] = s;
   }
   __syncthreads();

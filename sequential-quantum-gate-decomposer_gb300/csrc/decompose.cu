@@ -455,14 +455,14 @@ __device__ __noinline__ double dec_eval(const DecArgs& a, const Sh& sh, const do
 // evaluation budget a.max_calls applies to this run (a new BFGS_Powell with its own call
 // count per restart, optimization_engines/BFGS.cpp:121-125); calls and iters accumulate
 // over the runs of the decomposition.
-template <int FORM>
-__device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, int& iters) {
+template <int FORM, class ZA>
+__device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, int& iters, const ZA& za) {
   int run = 0;
   const int P = a.P;
   double* Z = sh.Z;
   const BfgsVecs bv = {sh.Z, sh.x, sh.x0, sh.g, sh.g0, sh.gbest, sh.d, sh.delta, sh.gamma, sh.v, sh.vp, sh.cs,
                        sh.ztg, sh.zs, sh.S, sh.sdv, sh.nz, sh.gtz, sh.redd, sh.scratch};
-  for (int i = threadIdx.x; i < P * P; i += blockDim.x) Z[i] = (i % (P + 1)) == 0 ? 1.0 : 0.0;
+  for (int i = threadIdx.x; i < P * P; i += blockDim.x) za.st(Z + i, (i % (P + 1)) == 0 ? 1.0 : 0.0);
   double norm_Z = -1.0;
   double f = dec_eval<FORM>(a, sh, sh.x, sh.g, b);
   calls++;
@@ -477,7 +477,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
   double fprev = fabs(f + f + 1.0);
   for (;;) {
     double dg, max_step, gn;
-    bfgs_direction(P, bv, dg, max_step, gn);
+    bfgs_direction(P, bv, dg, max_step, gn, za);
     if (gn <= 1e-19 * 1e-19 || dg >= 0.0 || f >= fprev) break;
     fprev = f;
     if (run >= a.max_calls) break;
@@ -536,7 +536,7 @@ __device__ double dec_bfgs(const DecArgs& a, const Sh& sh, int b, int& calls, in
       __syncthreads();
     }
     if (step == 0.0) break;
-    norm_Z = bfgs_update(P, bv, norm_Z);
+    norm_Z = bfgs_update(P, bv, norm_Z, za);
   }
   return f;
 }
@@ -661,8 +661,10 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_env_costgrad(DecArgs a, cons
 
 // At most 80 registers (6 CTAs of 128 threads per SM): the evaluation keeps only one warp
 // per CTA busy at n = 3, so resident CTAs are what hides FP64 and shared-memory latency
-// (measured 7470 vs 7103 decompositions/s with the unconstrained 126 registers).
-template <int OPT, int FORM>
+// (measured 7470 vs 7103 decompositions/s with the unconstrained 126 registers).  ZG: the
+// BFGS matrices live in global slots and are accessed with the L2 evict_last policy
+// (ZKeepL2); otherwise they are in shared memory (or absent, for ADAM).
+template <int OPT, int FORM, bool ZG>
 __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
   extern __shared__ double2 smem2[];
   const int b = blockIdx.x;
@@ -678,6 +680,14 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     dec_vec = (int*)take(sizeof(int) * 20);
     sh.Z = nullptr;
   } else if (a.z_in_smem) {
+    if constexpr (ZG) {  // the L2-kept accessors need Z in global memory: not this launch
+      if (threadIdx.x == 0) {
+        a.cost[b] = __longlong_as_double(0x7ff8000000000000LL);
+        a.calls[b] = -1;
+        if (a.iters) a.iters[b] = -1;
+      }
+      return;
+    }
     sh.Z = (double*)take(sizeof(double) * P * P);
   } else {
     __shared__ int z_slot;
@@ -719,7 +729,11 @@ __global__ void __launch_bounds__(kDecThreads, 6) k_decompose(DecArgs a) {
     for (int loop = 0; loop < a.loops; loop++) {
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.x[i] = sh.guess[i];
       __syncthreads();
-      double f = dec_bfgs<FORM>(a, sh, b, calls, iters);
+      double f;
+      if constexpr (ZG)
+        f = dec_bfgs<FORM>(a, sh, b, calls, iters, ZKeepL2());
+      else
+        f = dec_bfgs<FORM>(a, sh, b, calls, iters, ZMem{});
       for (int i = threadIdx.x; i < P; i += blockDim.x) sh.guess[i] = sh.x[i];
       __syncthreads();
       if (f < best) {
@@ -886,48 +900,58 @@ int two_chain_split(const sqg_circuit& c) {
 }
 
 // Kernel attributes and launch shared by the BFGS and ADAM entry points.
-template <int OPT, int FORM>
+template <int OPT, int FORM, bool ZG>
 int dec_launch_form(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   cudaFuncAttributes fa = {};
-  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_decompose<OPT, FORM>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_decompose<OPT, FORM, ZG>);
   if (e == cudaSuccess && smem + fa.sharedSizeBytes > (size_t)optin)
     return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the batched decomposition kernel");
   // raised to the device maximum (less the kernel's static shared memory), never lowered:
   // the attribute is shared by all callers
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_decompose<OPT, FORM, ZG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              optin - (int)fa.sharedSizeBytes);
   if (e != cudaSuccess) {
     cudaGetLastError();  // leave no error behind for the next launch to report
     return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
   }
-  k_decompose<OPT, FORM><<<batch, dec_threads(c), smem, (cudaStream_t)stream>>>(a);
+  k_decompose<OPT, FORM, ZG><<<batch, dec_threads(c), smem, (cudaStream_t)stream>>>(a);
   e = cudaGetLastError();
   return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_decompose: ") + cudaGetErrorString(e));
 }
 
-template <int OPT>
-int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
-  if (a.chains == 2) return dec_launch_form<OPT, kFormTwoChains>(c, a, batch, smem, stream);
-  if (a.cyclic) return dec_launch_form<OPT, kFormCyclic>(c, a, batch, smem, stream);
-  return dec_launch_form<OPT, kFormSweep>(c, a, batch, smem, stream);
+template <int OPT, bool ZG>
+int dec_launch_z(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
+  if (a.chains == 2) return dec_launch_form<OPT, kFormTwoChains, ZG>(c, a, batch, smem, stream);
+  if (a.cyclic) return dec_launch_form<OPT, kFormCyclic, ZG>(c, a, batch, smem, stream);
+  return dec_launch_form<OPT, kFormSweep, ZG>(c, a, batch, smem, stream);
 }
 
-template <int OPT, int FORM>
+// BFGS with its matrices in global slots runs the ZG kernels (L2-kept Z accesses).
+template <int OPT>
+int dec_launch(const sqg_circuit* c, const DecArgs& a, int batch, size_t smem, void* stream) {
+  if constexpr (OPT == kBfgs) {
+    if (!a.z_in_smem) return dec_launch_z<OPT, true>(c, a, batch, smem, stream);
+  }
+  return dec_launch_z<OPT, false>(c, a, batch, smem, stream);
+}
+
+template <int OPT, int FORM, bool ZG>
 int dec_max_active_per_sm(const sqg_circuit* c, size_t smem) {
   int dev = 0, optin = 0, nb = 0;
   cudaFuncAttributes fa = {};
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
-  if (cudaFuncGetAttributes(&fa, k_decompose<OPT, FORM>) != cudaSuccess) return 0;
+  if (cudaFuncGetAttributes(&fa, k_decompose<OPT, FORM, ZG>) != cudaSuccess) return 0;
   if (smem + fa.sharedSizeBytes > (size_t)optin) return 0;
-  if (cudaFuncSetAttribute(k_decompose<OPT, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(k_decompose<OPT, FORM, ZG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            optin - (int)fa.sharedSizeBytes) != cudaSuccess)
     return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_decompose<OPT, FORM>, dec_threads(c), smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_decompose<OPT, FORM, ZG>, dec_threads(c), smem) !=
+      cudaSuccess)
     return 0;
   return nb;
 }
@@ -937,9 +961,9 @@ int dec_max_active_per_sm(const sqg_circuit* c, size_t smem) {
 // instance (one per instance if the occupancy cannot be queried).
 int dec_z_slots(const sqg_circuit* c, int cols, int batch) {
   const size_t smem = dec_smem_bytes(c, cols, false);
-  int per_sm = std::max(dec_max_active_per_sm<kBfgs, kFormSweep>(c, smem),
-                        std::max(dec_max_active_per_sm<kBfgs, kFormCyclic>(c, smem),
-                                 dec_max_active_per_sm<kBfgs, kFormTwoChains>(c, smem)));
+  int per_sm = std::max(dec_max_active_per_sm<kBfgs, kFormSweep, true>(c, smem),
+                        std::max(dec_max_active_per_sm<kBfgs, kFormCyclic, true>(c, smem),
+                                 dec_max_active_per_sm<kBfgs, kFormTwoChains, true>(c, smem)));
   cudaGetLastError();  // a failed query leaves no error behind
   int dev = 0, sms = 0;
   if (per_sm <= 0 || cudaGetDevice(&dev) != cudaSuccess ||

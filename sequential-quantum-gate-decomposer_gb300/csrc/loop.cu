@@ -331,14 +331,14 @@ __global__ void __launch_bounds__(kLoopThreads) k_bfgs_loop_step(BfgsLoopArgs a,
     if (s.step == 0.0) {
       run_over = true;
     } else {
-      s.norm_Z = bfgs_update(P, v, s.norm_Z);
+      s.norm_Z = bfgs_update(P, v, s.norm_Z, ZMem{});
       direction = true;
     }
   }
   bool search = !ls_end && !run_over && !direction;  // the line search goes on at s.step
   if (direction) {
     double dg, max_step, gn;
-    bfgs_direction(P, v, dg, max_step, gn);
+    bfgs_direction(P, v, dg, max_step, gn, ZMem{});
     if (gn <= 1e-19 * 1e-19 || dg >= 0.0 || s.f >= s.fprev) {
       run_over = true;
     } else {
