@@ -1,6 +1,7 @@
 """State-vector application (sqg_apply_state, up to 30 qubits) against the oracle: fused
 blocks and one pass per gate, batches, the drop-in Circuit.apply_to on 1-D states, and at
-sizes the oracle cannot reach, size-independent properties (norm, fused == unfused)."""
+sizes the oracle cannot reach, size-independent properties (norm, fused == unfused, a circuit
+followed by its adjoint giving the state back at 27 and 30 qubits)."""
 import importlib
 
 import numpy as np
@@ -160,3 +161,61 @@ def test_second_renyi_entropy(sqg, wl):
     rho = M @ M.conj().T
     want = -np.log(np.sum(np.abs(rho) ** 2))
     assert np.isclose(c.get_Second_Renyi_Entropy(th, psi, keep), want, atol=1e-10)
+
+
+def _inverse(sqg, c, theta):
+    """The adjoint circuit: gates in reverse order, each inverted through its parameters (U3
+    with stored (t, p, l) -> (-t, -l, -p); RX, RY, RZ, CRY negated; CNOT, CZ their own inverse)."""
+    inv = sqg.Circuit(c.qbit_num)
+    recs = c.gate_records()
+    params = []
+    for t, tg, ctl, ps in recs[::-1]:
+        t, tg, ctl, ps = int(t), int(tg), int(ctl), int(ps)
+        if t == sqg.U3:
+            inv.add_U3(tg)
+            params += [-theta[ps], -theta[ps + 2], -theta[ps + 1]]
+        elif t in (sqg.RX, sqg.RY, sqg.RZ):
+            getattr(inv, {sqg.RX: "add_RX", sqg.RY: "add_RY", sqg.RZ: "add_RZ"}[t])(tg)
+            params.append(-theta[ps])
+        elif t == sqg.CRY:
+            inv.add_CRY(tg, ctl)
+            params.append(-theta[ps])
+        else:
+            getattr(inv, "add_CNOT" if t == sqg.CNOT else "add_CZ")(tg, ctl)
+    return inv, np.asarray(params, dtype=np.float64)
+
+
+@pytest.mark.parametrize("n", [27, 30])
+def test_largest_registers_round_trip(sqg, wl, n):
+    """At the largest registers (2^30 amplitudes, 16 GiB, the limit of sqg_apply_state) a
+    circuit of every gate kind followed by its adjoint gives back the state, fused and one pass
+    per gate, and the norm is kept: checks that index arithmetic holds up to the last qubit."""
+    rng = np.random.default_rng(300 + n)
+    c = wl.all_gates_circuit(n, 48, rng)
+    for q in (n - 1, n - 2, 0):  # gates on the highest qubits for certain
+        c.add_CRY(q, (q + 1) % n)
+        c.add_U3(q)
+    theta = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    inv, theta_inv = _inverse(sqg, c, theta)
+    th = torch.from_numpy(theta).cuda()
+    th_inv = torch.from_numpy(theta_inv).cuda()
+    N = 1 << n
+    psi = torch.empty(N, dtype=torch.complex128, device="cuda")
+    gen = torch.Generator(device="cuda").manual_seed(n)
+    psi.real.normal_(generator=gen)
+    psi.imag.normal_(generator=gen)
+    psi /= torch.linalg.vector_norm(psi)
+    head = slice(0, 1 << 20)
+    for fused in (True, False):
+        v = psi.clone()
+        c.apply_state_device(th, v, fused=fused)
+        assert abs(float(torch.linalg.vector_norm(v)) - 1.0) < 1e-12
+        assert float((v[head] - psi[head]).abs().max()) > 1e-6  # the circuit did act
+        inv.apply_state_device(th_inv, v, fused=fused)
+        v.sub_(psi)  # in place: at 30 qubits each full-size temporary is 16 GiB
+        torch.cuda.synchronize()
+        assert float(v.abs().max()) < 1e-12
+        del v
+        torch.cuda.empty_cache()
+    del psi
+    torch.cuda.empty_cache()
