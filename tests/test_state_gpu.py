@@ -219,3 +219,34 @@ def test_largest_registers_round_trip(sqg, wl, n):
         torch.cuda.empty_cache()
     del psi
     torch.cuda.empty_cache()
+
+
+def test_largest_matrix_register_round_trip(sqg, wl):
+    """13 qubits, the largest register of the matrix entry points (an 8192 x 8192 complex128
+    target, 1 GiB): a circuit of every gate kind followed by its adjoint gives back the matrix,
+    fused and one pass per gate."""
+    n = 13
+    rng = np.random.default_rng(313)
+    c = wl.all_gates_circuit(n, 40, rng)
+    c.add_CRY(n - 1, 0)
+    c.add_U3(n - 1)
+    theta = rng.uniform(0, 2 * np.pi, c.get_Parameter_Num())
+    inv, theta_inv = _inverse(sqg, c, theta)
+    th = torch.from_numpy(theta).cuda()
+    th_inv = torch.from_numpy(theta_inv).cuda()
+    N = 1 << n
+    m = torch.empty((N, N), dtype=torch.complex128, device="cuda")
+    gen = torch.Generator(device="cuda").manual_seed(n)
+    m.real.normal_(generator=gen)
+    m.imag.normal_(generator=gen)
+    for fused in (True, False):
+        v = m.clone()
+        c.apply_to_device(th, v, fused=fused)
+        assert float((v[:64] - m[:64]).abs().max()) > 1e-6
+        inv.apply_to_device(th_inv, v, fused=fused)
+        v.sub_(m)
+        torch.cuda.synchronize()
+        assert float(v.abs().max()) < 1e-11
+        del v
+    del m
+    torch.cuda.empty_cache()
