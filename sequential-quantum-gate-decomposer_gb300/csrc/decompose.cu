@@ -325,20 +325,23 @@ __device__ double dec_eval_cyclic2(const DecArgs& a, const Sh& sh, const double*
     if (gate_controlled(gs.type)) gs.control += n;
     return gs;
   };
-  if (warp == 0) {
-    for (int e = lane; e < NN; e += 32) mA[e] = sh.tgt[(e & (N - 1)) * N + (e >> n)];
+  // Each phase of each chain is one loop with one gate-application site (the gate, the side
+  // and the orientation are chosen per step), so the evaluation's code stays small: the eight
+  // CTAs of an SM run it and the BFGS update in different phases out of one instruction cache.
+  double2* const m = warp == 0 ? mA : mB;
+  if (warp < 2) {
+    for (int e = lane; e < NN; e += 32)
+      m[e] = warp == 0 ? sh.tgt[(e & (N - 1)) * N + (e >> n)]
+                       : make_double2((e & (N - 1)) == (e >> n) ? 1.0 : 0.0, 0.0);
     __syncwarp();
-    for (int k = 0; k < h; k++) {
-      const Gate gt = sh.gates[k];
-      tile_apply_by(mA, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[k], ORIENT_FWD), lane, 32);
-      __syncwarp();
-    }
-  } else if (warp == 1) {
-    for (int e = lane; e < NN; e += 32) mB[e] = make_double2((e & (N - 1)) == (e >> n) ? 1.0 : 0.0, 0.0);
-    __syncwarp();
-    for (int k = L - 1; k > h; k--) {
-      const Gate gs = shifted(k);
-      tile_apply_by(mB, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[k], ORIENT_TRANS), lane, 32);
+    // warp 0: psi_{h-1} = G_{h-1} ... G_0 T; warp 1: W = G_{L-1} ... G_{h+1} from the right
+    const int steps = warp == 0 ? h : L - 1 - h;
+#pragma unroll 1
+    for (int s = 0; s < steps; s++) {
+      const int k = warp == 0 ? s : L - 1 - s;
+      const Gate gt = warp == 0 ? sh.gates[k] : shifted(k);
+      tile_apply_by(m, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[k], warp == 0 ? ORIENT_FWD : ORIENT_TRANS), lane,
+                    32);
       __syncwarp();
     }
   }
@@ -362,19 +365,36 @@ __device__ double dec_eval_cyclic2(const DecArgs& a, const Sh& sh, const double*
     }
     asm volatile("bar.sync 2, 64;" ::: "memory");
   }
-  if (warp == 1) {
-    for (int k = h; k < L; k++) {
-      const Gate gt = sh.gates[k];
-      if (gate_param_num(gt.type) > 0) {
-        cyclic_overlap(mB, n, N, gt, sh.R + k * 8);
-        __syncwarp();
+  if (warp < 2) {
+    // warp 1, for k = h .. L-1: [overlap of G_k] [M <- G_k M, except k = L-1 > h] [trace at
+    // k = h] [M <- M G_{k+1}^dagger, k < L-1];  warp 0, for k = h-1 .. 0: [M <- G_k^dagger M]
+    // [M <- M G_{k+1}] [overlap of G_k].  Four sub-steps per gate, in that order.
+    const int gates = warp == 0 ? h : L - h;
+#pragma unroll 1
+    for (int s = 0; s < 4 * gates; s++) {
+      const int k = warp == 0 ? h - 1 - (s >> 2) : h + (s >> 2), sub = s & 3;
+      const bool param = gate_param_num(sh.gates[k].type) > 0;
+      int act = 0, gk = k, orient = ORIENT_FWD;  // act: 1 apply, 2 apply shifted, 3 overlap, 4 trace
+      bool right = false;
+      if (warp == 1) {
+        if (sub == 0 && param) act = 3;
+        else if (sub == 1 && (k == h || k < L - 1)) act = 1;
+        else if (sub == 2 && k == h) act = 4;
+        else if (sub == 3 && k < L - 1) { act = 1; right = true; gk = k + 1; orient = ORIENT_CONJ; }
+      } else {
+        if (sub == 0) { act = 1; orient = ORIENT_ADJ; }
+        else if (sub == 1) { act = 1; right = true; gk = k + 1; orient = ORIENT_TRANS; }
+        else if (sub == 2 && param) act = 3;
       }
-      if (k == h || k < L - 1) {
-        tile_apply_by(mB, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[k], ORIENT_FWD), lane, 32);
+      if (act == 1) {
+        const Gate gt = right ? shifted(gk) : sh.gates[gk];
+        tile_apply_by(m, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[gk], orient), lane, 32);
         __syncwarp();
-      }
-      if (k == h) {  // tr(G_h M_h) = tr(E^dagger U T)
-        double2 v = lane < N ? mB[lane * N + lane] : make_double2(0.0, 0.0);
+      } else if (act == 3) {
+        cyclic_overlap(m, n, N, sh.gates[k], sh.R + k * 8);
+        __syncwarp();
+      } else if (act == 4) {  // tr(G_h M_h) = tr(E^dagger U T)
+        double2 v = lane < N ? m[lane * N + lane] : make_double2(0.0, 0.0);
         for (int o = 1; o < N; o <<= 1) {
           v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
           v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
@@ -383,24 +403,6 @@ __device__ double dec_eval_cyclic2(const DecArgs& a, const Sh& sh, const double*
           sh.redd[0] = v.x;
           sh.redd[1] = v.y;
         }
-        __syncwarp();
-      }
-      if (k < L - 1) {
-        const Gate gs = shifted(k + 1);
-        tile_apply_by(mB, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[k + 1], ORIENT_CONJ), lane, 32);
-        __syncwarp();
-      }
-    }
-  } else if (warp == 0) {
-    for (int k = h - 1; k >= 0; k--) {
-      const Gate gt = sh.gates[k];
-      tile_apply_by(mA, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[k], ORIENT_ADJ), lane, 32);
-      __syncwarp();
-      const Gate gs = shifted(k + 1);
-      tile_apply_by(mA, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[k + 1], ORIENT_TRANS), lane, 32);
-      __syncwarp();
-      if (gate_param_num(gt.type) > 0) {
-        cyclic_overlap(mA, n, N, gt, sh.R + k * 8);
         __syncwarp();
       }
     }
