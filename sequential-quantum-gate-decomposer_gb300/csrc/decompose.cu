@@ -265,36 +265,50 @@ __device__ double dec_eval_cyclic(const DecArgs& a, const Sh& sh, const double* 
       tile_apply(m, NN, 2 * n, 1, gs, make_op(gs.type, sh.gm[g], orient));
       sweep_sync(aw);
     };
+#pragma unroll 1
     for (int g = L - 1; g >= 1; g--) right(g, ORIENT_TRANS);
-    for (int g = 0; g < L; g++) {
+    // for g = 0 .. L-1: [overlap of G_g] [M <- G_g M, except g = L-1 > 0] [trace at g = 0]
+    // [M <- M G_{g+1}^dagger, g < L-1], as a loop of four sub-steps per gate with one
+    // gate-application site (a small code footprint, as in dec_eval_cyclic2)
+#pragma unroll 1
+    for (int s = 0; s < 4 * L; s++) {
+      const int g = s >> 2, sub = s & 3;
       const Gate gt = sh.gates[g];
-      if (gate_param_num(gt.type) > 0) {
+      int act = 0, gk = g, orient = ORIENT_FWD;  // act: 1 apply, 2 overlap, 3 trace
+      bool shift = false;
+      if (sub == 0 && gate_param_num(gt.type) > 0) act = 2;
+      else if (sub == 1 && (g == 0 || g < L - 1)) act = 1;
+      else if (sub == 2 && g == 0) act = 3;
+      else if (sub == 3 && g < L - 1) { act = 1; shift = true; gk = g + 1; orient = ORIENT_CONJ; }
+      if (act == 1) {
+        Gate x = sh.gates[gk];
+        if (shift) {
+          x.target += n;
+          if (gate_controlled(x.type)) x.control += n;
+        }
+        tile_apply(m, NN, 2 * n, 1, x, make_op(x.type, sh.gm[gk], orient));
+        sweep_sync(aw);
+      } else if (act == 2) {
         if (threadIdx.x < 32) cyclic_overlap(m, n, N, gt, sh.R + g * 8);
         sweep_sync(aw);
-      }
-      if (g == 0 || g < L - 1) {
-        tile_apply(m, NN, 2 * n, 1, gt, make_op(gt.type, sh.gm[g], ORIENT_FWD));
+      } else if (act == 3) {
+        if (threadIdx.x < 32) {
+          const int lane = threadIdx.x;
+          double2 v = lane < N ? m[lane * N + lane] : make_double2(0.0, 0.0);
+          for (int i = lane + 32; i < N; i += 32) {  // N = 64: two diagonal entries per lane
+            v.x += m[i * N + i].x;
+            v.y += m[i * N + i].y;
+          }
+          for (int o = 1; o < min(N, 32); o <<= 1) {  // lanes 0..min(N, 32)-1 end with the full sum
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+          }
+          if (lane == 0) {
+            sh.redd[0] = v.x;
+            sh.redd[1] = v.y;
+          }
+        }
         sweep_sync(aw);
-      }
-      if (g == 0 && threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        double2 v = lane < N ? m[lane * N + lane] : make_double2(0.0, 0.0);
-        for (int i = lane + 32; i < N; i += 32) {  // N = 64: two diagonal entries per lane
-          v.x += m[i * N + i].x;
-          v.y += m[i * N + i].y;
-        }
-        for (int o = 1; o < min(N, 32); o <<= 1) {  // lanes 0..min(N, 32)-1 end with the full sum
-          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-        }
-        if (lane == 0) {
-          sh.redd[0] = v.x;
-          sh.redd[1] = v.y;
-        }
-      }
-      if (g < L - 1) {
-        if (g == 0) sweep_sync(aw);
-        right(g + 1, ORIENT_CONJ);
       }
     }
   }
