@@ -1053,8 +1053,18 @@ static int env_launch(const DecArgs& a, const double* theta, double* cost, doubl
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_env_costgrad<FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  if (e != cudaSuccess) return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  cudaFuncAttributes fa = {};
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_env_costgrad<FORM>);
+  if (e == cudaSuccess && smem + fa.sharedSizeBytes > (size_t)optin)
+    return set_error(SQG_ERR_UNSUPPORTED, "circuit too large for the environment-matrix evaluation");
+  // the dynamic maximum leaves room for any static shared memory of the kernel
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_env_costgrad<FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - (int)fa.sharedSizeBytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // leave no error behind for the next launch to report
+    return set_error(SQG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  }
   k_env_costgrad<FORM><<<a.B, threads, smem, s>>>(a, theta, cost, grad);
   e = cudaGetLastError();
   return e == cudaSuccess ? SQG_OK : set_error(SQG_ERR_CUDA, std::string("k_env_costgrad: ") + cudaGetErrorString(e));
